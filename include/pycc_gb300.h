@@ -1,0 +1,81 @@
+/* pycc_gb300 -- C ABI of the GB300-native RHF-CCSD amplitude engine.
+ *
+ * Every entry point takes raw device pointers (FP64 unless stated), element counts and
+ * element strides, plus a cudaStream_t passed as void* (NULL = legacy default stream).
+ * Work is enqueued asynchronously on that stream.  The return value is 0 on success and
+ * negative on a host-side argument/launch error; pcg_last_error() then holds the text.
+ *
+ * The reference (CrawfordGroup/pycc) is pure Python; each entry below names the reference
+ * function whose arithmetic it replaces.  The reference-side binding is shown in
+ * INTEGRATION.md.
+ */
+#ifndef PYCC_GB300_H
+#define PYCC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- library ------------------------------------------------------------------------- */
+const char* pcg_last_error(void);
+int pcg_abi_version(void);
+/* compute capability of the current device as major*10+minor (103 on GB300) */
+int pcg_device_cc(void);
+int pcg_stream_sync(void* stream);
+
+/* ---- FP64 strided contraction ---------------------------------------------------------
+ * Replaces ContractionBackend.__call__ (pycc/device.py:64-87), i.e. every pairwise
+ * self.contract(...) of the CCSD builders (pycc/ccwfn.py:432-945):
+ *   C[m,n] = beta*C[m,n] + alpha * sum_k A[m,k] * B[n,k]
+ * m, n, k are flat indices over up to 4 sub-indices each (outer first), given as extents
+ * and element strides: M sub-indices carry (stride in A, stride in C), N sub-indices
+ * (stride in B, stride in C), K sub-indices (stride in A, stride in B).  An empty group
+ * (count 0) is a single index of extent 1 (outer products, full dots). */
+int pcg_contract_f64(int m_n, const long long* m_ext, const long long* m_sa,
+                     const long long* m_sc, int n_n, const long long* n_ext,
+                     const long long* n_sb, const long long* n_sc, int k_n,
+                     const long long* k_ext, const long long* k_sa, const long long* k_sb,
+                     double alpha, const double* A, const double* B, double beta, double* C,
+                     void* stream);
+
+/* ---- FP64 elementwise kernels ---------------------------------------------------------- */
+/* tau_ijab = f1*t2_ijab + f2*t1_ia*t1_jb; CCwfn.build_tau (pycc/ccwfn.py:432-455) */
+int pcg_tau_f64(const double* t1, const double* t2, long long no, long long nv, double f1,
+                double f2, double* out, void* stream);
+
+/* out[p] = a*X[p] + b*Y[p] over a 4-index box with per-tensor strides (Y may be NULL);
+ * the operand combinations 2*t2 - t2.swapaxes(2,3) etc. (pycc/ccwfn.py:757,933-934) */
+int pcg_combine4_f64(const long long* ext4, double a, const double* X, const long long* xs4,
+                     double b, const double* Y, const long long* ys4, double* out,
+                     const long long* os4, void* stream);
+
+/* out_ijab = h_ijab + h_jiba (out != h); r_T2 symmetrisation (pycc/ccwfn.py:790) */
+int pcg_symmetrize_f64(const double* h, long long no, long long nv, double* out, void* stream);
+
+/* t1 += r1/Dia, t2 += r2/Dijab with D from eps[nmo]; *rms2 = sum (r/D)^2 (device scalar).
+ * work: >= 1024 doubles of device scratch.  solve_cc update (pycc/ccwfn.py:281-284) */
+int pcg_update_amps_f64(double* t1, double* t2, const double* r1, const double* r2,
+                        const double* eps, long long no, long long nv, double* work,
+                        long long work_len, double* rms2, void* stream);
+
+/* *out = 2 sum f_ia t_ia + sum (t2_ijab + t_ia t_jb) L_ijab (device scalar); f: o x v with
+ * strides fs[2], L: oovv with strides ls[4]; work >= 1024 doubles.
+ * CCwfn.cc_energy (pycc/ccwfn.py:1122-1162) */
+int pcg_energy_f64(const double* fov, const long long* fs2, const double* L,
+                   const long long* ls4, const double* t1, const double* t2, long long no,
+                   long long nv, double* work, long long work_len, double* out, void* stream);
+
+/* out[j] = <x, ys[j]>, 1 <= k <= 16 (ys: host array of device pointers); work >= 1024*k
+ * doubles.  DIIS overlaps, helper_diis.extrapolate (pycc/utils.py:330-339) */
+int pcg_dots_f64(const double* x, const double* const* ys, int k, long long n, double* work,
+                 long long work_len, double* out, void* stream);
+
+/* out = sum_j c[j]*xs[j], 1 <= k <= 16 (xs, c on the host; out must not alias an input).
+ * DIIS extrapolation, helper_diis.extrapolate (pycc/utils.py:351-355) */
+int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n, double* out,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PYCC_GB300_H */

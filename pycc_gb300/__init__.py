@@ -1,0 +1,16 @@
+"""pycc_gb300 -- a GB300-native RHF-CCSD amplitude engine.
+
+Drop-in for the residual iteration of CrawfordGroup/pycc's ``CCwfn`` (``pycc/ccwfn.py``)
+running on hand-written sm_103a CUDA kernels behind a C ABI (``include/pycc_gb300.h``).
+"""
+from .exceptions import PyCCError, InvalidKeywordError, ConvergenceError, NumericalError
+from .hamiltonian import Hamiltonian, BlockTensor
+from .synth import SyntheticFactors, CONFIGS, synthetic_factors
+from .ccwfn import CCwfn, ccwfn
+from .contract import ContractionBackend, contract_f64
+
+__all__ = [
+    "CCwfn", "ccwfn", "Hamiltonian", "BlockTensor", "SyntheticFactors", "CONFIGS",
+    "synthetic_factors", "ContractionBackend", "contract_f64", "PyCCError",
+    "InvalidKeywordError", "ConvergenceError", "NumericalError",
+]

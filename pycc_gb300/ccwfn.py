@@ -1,0 +1,377 @@
+"""GPU RHF-CCSD amplitude engine with the reference's ``CCwfn`` interface.
+
+Drop-in for the residual iteration of CrawfordGroup/pycc's ``CCwfn`` (``pycc/ccwfn.py``):
+the same method names, argument orders and return layouts -- ``build_tau``,
+``build_Fae/Fmi/Fme``, ``build_Wmnij/Wmbej/Wmbje/Zmbij``, ``r_T1``, ``r_T2``, ``residuals``,
+``cc_energy`` and ``solve_cc`` -- executed by the CUDA library ``libpycc_gb300.so``:
+
+* ``precision='DP'``: every pairwise contraction is one launch of the FP64 strided DMMA
+  kernel (``pcg_contract_f64``) through ``self.contract``; tau builds, the r2
+  symmetrisation, the Jacobi update with its norm and the energy are fused FP64 kernels.
+* ``precision='MIXED'``: the residual runs on the tcgen05 tensor-core engine
+  (``pycc_gb300.mixed``): BF16 operands with FP32 accumulation (FP8 with per-row scales for
+  the <ab|ef> ladder), switching to compensated split-BF16x3 products once the update norm
+  drops below ``switch_threshold``; amplitudes, denominators, energy, norms and DIIS stay FP64.
+* ``precision='SP'``: every contraction in split-BF16x3 (single-precision class accuracy),
+  FP64 amplitudes.
+
+There is no CPU fallback: ``device='CPU'`` is the reference's own code path.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .contract import ContractionBackend
+from .diis import DIIS
+from .exceptions import ConvergenceError, InvalidKeywordError, NumericalError, PyCCError
+from .hamiltonian import Hamiltonian
+
+WORK_LEN = 4096
+
+
+def _ptr(t):
+    return t.data_ptr()
+
+
+class CCwfn:
+    """RHF-CCSD wave function on one GPU (mirrors ``pycc/ccwfn.py:32-213``).
+
+    Parameters
+    ----------
+    scf_wfn : Hamiltonian or object with an ``H`` attribute
+        The MO Hamiltonian (see :class:`pycc_gb300.Hamiltonian`); replaces the psi4 SCF
+        wave function the reference reads its integrals from.
+    model : 'CCSD' or 'CCSD(T)'
+    device : 'GPU'
+    precision : 'DP', 'SP' or 'MIXED'
+    switch_threshold : float
+        MIXED only: update norm below which contractions switch to split-BF16x3.
+    vvvv_fp8 : bool
+        MIXED only: run the <ab|ef> ladder in FP8 before the switch.
+    """
+
+    VALID_MODELS = ['CCD', 'CC2', 'CCSD', 'CCSD(T)', 'CC3']
+    SUPPORTED_MODELS = ['CCSD', 'CCSD(T)']
+
+    def __init__(self, scf_wfn, **kwargs):
+        time_init = time.time()
+        model = kwargs.pop('model', 'CCSD').upper()
+        if model not in self.VALID_MODELS:
+            raise InvalidKeywordError('model', model, self.VALID_MODELS)
+        if model not in self.SUPPORTED_MODELS:
+            raise NotImplementedError("pycc_gb300 runs the RHF CCSD / CCSD(T) path only (got %r)" % model)
+        self.model = model
+        device = kwargs.pop('device', 'GPU').upper()
+        if device not in ('CPU', 'GPU'):
+            raise InvalidKeywordError('device', device, ['CPU', 'GPU'])
+        if device == 'CPU':
+            raise NotImplementedError("pycc_gb300 is the GPU engine; device='CPU' is the reference's path")
+        self.device = device
+        precision = kwargs.pop('precision', 'DP').upper()
+        if precision not in ('DP', 'SP', 'MIXED'):
+            raise InvalidKeywordError('precision', precision, ['DP', 'SP', 'MIXED'])
+        self.precision = precision
+        self.switch_threshold = float(kwargs.pop('switch_threshold', 1e-5))
+        self.vvvv_fp8 = bool(kwargs.pop('vvvv_fp8', True))
+        self.quiet = bool(kwargs.pop('quiet', True))
+        orbital_basis = kwargs.pop('orbital_basis', 'spatial')
+        if orbital_basis != 'spatial':
+            raise NotImplementedError("pycc_gb300 runs the closed-shell spatial-orbital path only")
+        self.orbital_basis = orbital_basis
+        local = kwargs.pop('local', None)
+        if local is not None:
+            raise NotImplementedError("local correlation is not part of the GPU engine")
+        self.local = None
+        if kwargs:
+            raise PyCCError("Unknown keyword argument(s): %s" % ", ".join(sorted(kwargs)))
+
+        H = scf_wfn if isinstance(scf_wfn, Hamiltonian) else getattr(scf_wfn, 'H', None)
+        if not isinstance(H, Hamiltonian):
+            raise TypeError("CCwfn needs a pycc_gb300.Hamiltonian (or an object carrying one as .H)")
+        _lib.load()
+        self.H = H
+        self.no, self.nv, self.nmo = H.no, H.nv, H.nmo
+        self.nfzc = 0
+        self.eref = float(getattr(scf_wfn, 'eref', 0.0))
+        self.o = slice(0, self.no)
+        self.v = slice(self.no, self.nmo)
+        self.device1 = H.device
+        self.stream = None
+        self.contract = ContractionBackend(self.device1, self.stream)
+        self._work = torch.empty(WORK_LEN, dtype=torch.float64, device=self.device1)
+        self._scalars = torch.zeros(8, dtype=torch.float64, device=self.device1)
+
+        no, nv = self.no, self.nv
+        eps = H.eps
+        eps_o, eps_v = eps[:no], eps[no:]
+        self.Dijab = (eps_o.reshape(-1, 1, 1, 1) + eps_o.reshape(-1, 1, 1)
+                      - eps_v.reshape(-1, 1) - eps_v)
+        self.Dia = eps_o.reshape(-1, 1) - eps_v
+        # amplitudes live in one flat FP64 vector [t1 | t2] (the DIIS vector)
+        self._amps = torch.zeros(no * nv + no * no * nv * nv, dtype=torch.float64,
+                                 device=self.device1)
+        self.t2.copy_(H.ERI[self.o, self.o, self.v, self.v] / self.Dijab)
+        self._mixed = None
+        self.ecc = None
+        self.niter = 0
+        self.timing = {"init": time.time() - time_init}
+
+    # -- amplitude views ------------------------------------------------------------------
+    @property
+    def t1(self):
+        no, nv = self.no, self.nv
+        return self._amps[:no * nv].view(no, nv)
+
+    @t1.setter
+    def t1(self, value):
+        self.t1.copy_(value)
+
+    @property
+    def t2(self):
+        no, nv = self.no, self.nv
+        return self._amps[no * nv:].view(no, no, nv, nv)
+
+    @t2.setter
+    def t2(self, value):
+        self.t2.copy_(value)
+
+    def _st(self):
+        return _lib.stream_handle(self.stream)
+
+    # -- pycc/ccwfn.py:432-455 ------------------------------------------------------------
+    def build_tau(self, t1, t2, fact1=1.0, fact2=1.0):
+        """tau_ijab = fact1 t2_ijab + fact2 t_ia t_jb (fused FP64 kernel)."""
+        t1 = t1.contiguous()
+        t2 = t2.contiguous()
+        out = torch.empty_like(t2)
+        _lib.call("pcg_tau_f64", _ptr(t1), _ptr(t2), self.no, self.nv, float(fact1), float(fact2),
+                  _ptr(out), self._st())
+        return out
+
+    def _combine(self, a, X, b, Y, perm_y, out=None):
+        """out_pqrs = a X_pqrs + b Y_perm (4-index; perm_y permutes Y's axes)."""
+        ext = list(X.shape)
+        if out is None:
+            out = torch.empty(ext, dtype=torch.float64, device=X.device)
+        ys = [0, 0, 0, 0]
+        if Y is not None:
+            Yp = Y.permute(*perm_y)
+            ys = list(Yp.stride())
+        _lib.call("pcg_combine4_f64", _lib.i64s(ext), float(a), _ptr(X), _lib.i64s(X.stride()),
+                  float(b), _ptr(Y) if Y is not None else None, _lib.i64s(ys), _ptr(out),
+                  _lib.i64s(out.stride()), self._st())
+        return out
+
+    # -- pycc/ccwfn.py:458-498 ------------------------------------------------------------
+    def build_Fae(self, o, v, F, L, t1, t2):
+        c = self.contract
+        Fae = F[v, v].clone()
+        c('me,ma->ae', F[o, v], t1, out=Fae, alpha=-0.5, beta=1.0)
+        c('mf,mafe->ae', t1, L[o, v, v, v], out=Fae, beta=1.0)
+        c('mnaf,mnef->ae', self.build_tau(t1, t2, 1.0, 0.5), L[o, o, v, v], out=Fae, alpha=-1.0,
+          beta=1.0)
+        return Fae
+
+    # -- pycc/ccwfn.py:501-534 ------------------------------------------------------------
+    def build_Fmi(self, o, v, F, L, t1, t2):
+        c = self.contract
+        Fmi = F[o, o].clone()
+        c('ie,me->mi', t1, F[o, v], out=Fmi, alpha=0.5, beta=1.0)
+        c('ne,mnie->mi', t1, L[o, o, o, v], out=Fmi, beta=1.0)
+        c('inef,mnef->mi', self.build_tau(t1, t2, 1.0, 0.5), L[o, o, v, v], out=Fmi, beta=1.0)
+        return Fmi
+
+    # -- pycc/ccwfn.py:537-565 ------------------------------------------------------------
+    def build_Fme(self, o, v, F, L, t1):
+        Fme = F[o, v].clone()
+        self.contract('nf,mnef->me', t1, L[o, o, v, v], out=Fme, beta=1.0)
+        return Fme
+
+    # -- pycc/ccwfn.py:568-604 ------------------------------------------------------------
+    def build_Wmnij(self, o, v, ERI, t1, t2):
+        c = self.contract
+        W = ERI[o, o, o, o].clone()
+        c('je,mnie->mnij', t1, ERI[o, o, o, v], out=W, beta=1.0)
+        c('ie,mnej->mnij', t1, ERI[o, o, v, o], out=W, beta=1.0)
+        c('ijef,mnef->mnij', self.build_tau(t1, t2), ERI[o, o, v, v], out=W, beta=1.0)
+        return W
+
+    # -- pycc/ccwfn.py:607-646 ------------------------------------------------------------
+    def build_Wmbej(self, o, v, ERI, L, t1, t2):
+        c = self.contract
+        W = ERI[o, v, v, o].clone()
+        c('jf,mbef->mbej', t1, ERI[o, v, v, v], out=W, beta=1.0)
+        c('nb,mnej->mbej', t1, ERI[o, o, v, o], out=W, alpha=-1.0, beta=1.0)
+        c('jnfb,mnef->mbej', self.build_tau(t1, t2, 0.5, 1.0), ERI[o, o, v, v], out=W, alpha=-1.0,
+          beta=1.0)
+        c('njfb,mnef->mbej', t2, L[o, o, v, v], out=W, alpha=0.5, beta=1.0)
+        return W
+
+    # -- pycc/ccwfn.py:649-684 ------------------------------------------------------------
+    def build_Wmbje(self, o, v, ERI, t1, t2):
+        c = self.contract
+        W = self._combine(-1.0, ERI[o, v, o, v], 0.0, None, None)
+        c('jf,mbfe->mbje', t1, ERI[o, v, v, v], out=W, alpha=-1.0, beta=1.0)
+        c('nb,mnje->mbje', t1, ERI[o, o, o, v], out=W, beta=1.0)
+        c('jnfb,mnfe->mbje', self.build_tau(t1, t2, 0.5, 1.0), ERI[o, o, v, v], out=W, beta=1.0)
+        return W
+
+    # -- pycc/ccwfn.py:687-715 ------------------------------------------------------------
+    def build_Zmbij(self, o, v, ERI, t1, t2):
+        return self.contract('mbef,ijef->mbij', ERI[o, v, v, v], self.build_tau(t1, t2))
+
+    # -- pycc/ccwfn.py:718-761 ------------------------------------------------------------
+    def r_T1(self, o, v, F, ERI, L, t1, t2, Fae, Fme, Fmi):
+        c = self.contract
+        r = F[v, o].transpose(0, 1).contiguous()
+        c('ie,ae->ia', t1, Fae, out=r, beta=1.0)
+        c('mi,ma->ia', Fmi, t1, out=r, alpha=-1.0, beta=1.0)
+        t2s = self._combine(2.0, t2, -1.0, t2, (0, 1, 3, 2))
+        c('imae,me->ia', t2s, Fme, out=r, beta=1.0)
+        c('nf,nafi->ia', t1, L[o, v, v, o], out=r, beta=1.0)
+        c('mief,maef->ia', t2s, ERI[o, v, v, v], out=r, beta=1.0)
+        c('mnae,nmei->ia', t2, L[o, o, v, o], out=r, alpha=-1.0, beta=1.0)
+        return r
+
+    # -- pycc/ccwfn.py:764-791, :886-945 --------------------------------------------------
+    def r_T2(self, o, v, F, ERI, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij):
+        r = self._r_T2_half(o, v, F, ERI, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij)
+        out = torch.empty_like(r)
+        _lib.call("pcg_symmetrize_f64", _ptr(r), self.no, self.nv, _ptr(out), self._st())
+        return out
+
+    def _r_T2_half(self, o, v, F, ERI, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij):
+        c = self.contract
+        r = self._combine(0.5, ERI[v, v, o, o].permute(2, 3, 0, 1), 0.0, None, None)
+        c('ijae,eb->ijab', t2, Fae.T, out=r, beta=1.0)
+        tmp = c('bm,me->be', t1.T, Fme)
+        c('ijae,eb->ijab', t2, tmp.T, out=r, alpha=-0.5, beta=1.0)
+        c('imab,mj->ijab', t2, Fmi, out=r, alpha=-1.0, beta=1.0)
+        tmp = c('je,em->jm', t1, Fme.T)
+        c('imab,mj->ijab', t2, tmp.T, out=r, alpha=-0.5, beta=1.0)
+        tau = self.build_tau(t1, t2)
+        c('mnab,mnij->ijab', tau, Wmnij, out=r, alpha=0.5, beta=1.0)
+        c('ijef,abef->ijab', tau, ERI[v, v, v, v], out=r, alpha=0.5, beta=1.0)
+        c('ma,mbij->ijab', t1, Zmbij, out=r, alpha=-1.0, beta=1.0)
+        c('imae,mbej->ijab', self._combine(1.0, t2, -1.0, t2, (0, 1, 3, 2)), Wmbej, out=r, beta=1.0)
+        c('imae,mbej->ijab', t2, self._combine(1.0, Wmbej, 1.0, Wmbje, (0, 1, 3, 2)), out=r,
+          beta=1.0)
+        c('mjae,mbie->ijab', t2, Wmbje, out=r, beta=1.0)
+        tmp = c('ie,ma->imea', t1, t1)          # t_ie t_ma
+        c('imea,mbej->ijab', tmp, ERI[o, v, v, o], out=r, alpha=-1.0, beta=1.0)
+        c('imeb,maje->ijab', tmp, ERI[o, v, o, v], out=r, alpha=-1.0, beta=1.0)
+        c('ie,abej->ijab', t1, ERI[v, v, v, o], out=r, beta=1.0)
+        c('ma,mbij->ijab', t1, ERI[o, v, o, o], out=r, alpha=-1.0, beta=1.0)
+        return r
+
+    # -- pycc/ccwfn.py:321-372 ------------------------------------------------------------
+    def residuals(self, F, t1, t2, real_time=False):
+        """(r1, r2) for the current amplitudes; r2 symmetrised, FP64 on the GPU."""
+        if real_time:
+            raise NotImplementedError("real-time (complex) residuals are not part of the GPU engine")
+        if self.precision in ('MIXED', 'SP'):
+            return self.mixed_engine().residuals(F, t1, t2)
+        o, v = self.o, self.v
+        ERI, L = self.H.ERI, self.H.L
+        Fae = self.build_Fae(o, v, F, L, t1, t2)
+        Fmi = self.build_Fmi(o, v, F, L, t1, t2)
+        Fme = self.build_Fme(o, v, F, L, t1)
+        Wmnij = self.build_Wmnij(o, v, ERI, t1, t2)
+        Wmbej = self.build_Wmbej(o, v, ERI, L, t1, t2)
+        Wmbje = self.build_Wmbje(o, v, ERI, t1, t2)
+        Zmbij = self.build_Zmbij(o, v, ERI, t1, t2)
+        r1 = self.r_T1(o, v, F, ERI, L, t1, t2, Fae, Fme, Fmi)
+        r2 = self.r_T2(o, v, F, ERI, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij)
+        return r1, r2
+
+    def mixed_engine(self):
+        if self._mixed is None:
+            from .mixed import MixedResidual
+            self._mixed = MixedResidual(self, mode='bf16x3' if self.precision == 'SP' else 'auto')
+        return self._mixed
+
+    # -- pycc/ccwfn.py:1122-1162 ----------------------------------------------------------
+    def cc_energy(self, o, v, F, L, t1, t2, out=None):
+        """E = 2 f_ia t_ia + tau_ijab L_ijab as a 0-d FP64 GPU tensor (fused kernel)."""
+        t1 = t1.contiguous()
+        t2 = t2.contiguous()
+        Fov = F[o, v]
+        Loovv = L[o, o, v, v]
+        if out is None:
+            out = torch.empty((), dtype=torch.float64, device=t2.device)
+        _lib.call("pcg_energy_f64", _ptr(Fov), _lib.i64s(Fov.stride()), _ptr(Loovv),
+                  _lib.i64s(Loovv.stride()), _ptr(t1), _ptr(t2), self.no, self.nv,
+                  _ptr(self._work), self._work.numel(), _ptr(out), self._st())
+        return out
+
+    def update_amplitudes(self, r1, r2):
+        """t1 += r1/Dia, t2 += r2/Dijab in place; returns rms = ||(r1/Dia, r2/Dijab)||_2."""
+        out = self._scalars[1:2]
+        _lib.call("pcg_update_amps_f64", _ptr(self.t1), _ptr(self.t2), _ptr(r1.contiguous()),
+                  _ptr(r2.contiguous()), _ptr(self.H.eps), self.no, self.nv, _ptr(self._work),
+                  self._work.numel(), _ptr(out), self._st())
+        return out
+
+    # -- pycc/ccwfn.py:216-319 ------------------------------------------------------------
+    def solve_cc(self, e_conv=1e-7, r_conv=1e-7, maxiter=100, max_diis=8, start_diis=1,
+                 callback=None):
+        """Jacobi + DIIS iteration to convergence; returns the correlation energy (float).
+
+        Raises :class:`ConvergenceError` if ``maxiter`` is exhausted and
+        :class:`NumericalError` if the energy or the update norm turns NaN/Inf.
+        """
+        t_start = time.time()
+        self.e_conv, self.r_conv, self.maxiter = e_conv, r_conv, maxiter
+        o, v, F, L = self.o, self.v, self.H.F, self.H.L
+        ecc = float(self.cc_energy(o, v, F, L, self.t1, self.t2))
+        self.energies = [ecc]
+        self.iter_times = []
+        diis = DIIS(self._amps, max_diis, self.stream)
+        ediff, rms = -ecc, float('inf')
+        for niter in range(1, maxiter + 1):
+            t0 = time.time()
+            ecc_last = ecc
+            if self._mixed is not None or self.precision in ('MIXED', 'SP'):
+                self.mixed_engine().select_mode(rms)
+            r1, r2 = self.residuals(F, self.t1, self.t2)
+            rms_t = self.update_amplitudes(r1, r2)
+            e_t = self.cc_energy(o, v, F, L, self.t1, self.t2)
+            del r1, r2
+            vals = torch.stack([e_t.reshape(()), rms_t.reshape(())]).cpu().numpy()
+            ecc, rms = float(vals[0]), math.sqrt(max(float(vals[1]), 0.0))
+            ediff = ecc - ecc_last
+            self.energies.append(ecc)
+            self.iter_times.append(time.time() - t0)
+            self.niter = niter
+            if not (math.isfinite(ecc) and math.isfinite(rms)):
+                raise NumericalError("non-finite energy/update norm at iteration %d" % niter)
+            if callback is not None:
+                callback(niter, ecc, ediff, rms)
+            if not self.quiet:
+                print("%4d  %20.15f  %12.3e  %12.3e" % (niter, ecc, ediff, rms))
+            if abs(ediff) < e_conv and rms < r_conv:
+                if self.precision != 'DP' and not self.mixed_engine().is_final_mode():
+                    # converged in a low-precision mode: continue in the compensated mode
+                    self.mixed_engine().force_final()
+                else:
+                    self.ecc = ecc
+                    self.timing["solve"] = time.time() - t_start
+                    if self.model == 'CCSD(T)':
+                        from .triples import t_energy
+                        et = t_energy(self)
+                        self.et = et
+                        ecc = ecc + et
+                        self.ecc = ecc
+                    return ecc
+            diis.add_error_vector(self._amps)
+            if niter >= start_diis:
+                self._amps.copy_(diis.extrapolate(self._amps))
+        raise ConvergenceError("CCSD", maxiter, ediff, rms)
+
+
+ccwfn = CCwfn

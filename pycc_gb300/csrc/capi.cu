@@ -1,0 +1,41 @@
+// Library-wide C-ABI helpers: error text, version, device query.
+#include "common.cuh"
+#include <cstring>
+
+namespace pcg {
+static thread_local char g_err[512] = {0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+}  // namespace pcg
+
+extern "C" const char* pcg_last_error(void) { return pcg::g_err; }
+
+extern "C" int pcg_abi_version(void) { return 1; }
+
+// Compute capability of the current device as major*10+minor, or a negative CUDA error.
+extern "C" int pcg_device_cc(void) {
+  int dev = 0, ma = 0, mi = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    pcg::set_error("pcg_device_cc: %s", cudaGetErrorString(e));
+    return -(int)e;
+  }
+  cudaDeviceGetAttribute(&ma, cudaDevAttrComputeCapabilityMajor, dev);
+  cudaDeviceGetAttribute(&mi, cudaDevAttrComputeCapabilityMinor, dev);
+  return ma * 10 + mi;
+}
+
+// Blocks until the stream's work has finished; returns 0 or the CUDA error code.
+extern "C" int pcg_stream_sync(void* stream) {
+  cudaError_t e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    pcg::set_error("pcg_stream_sync: %s", cudaGetErrorString(e));
+    return (int)e;
+  }
+  return 0;
+}

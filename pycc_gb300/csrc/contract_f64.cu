@@ -1,0 +1,262 @@
+// FP64 strided tensor contraction on the FP64 tensor pipe (DMMA, mma.sync m8n8k4 f64).
+//
+//   C[m, n] = beta * C[m, n] + alpha * sum_k A[m, k] * B[n, k]
+//
+// m, n and k are flat indices over up to four sub-indices each; every sub-index carries
+// its own element stride in both tensors that hold it, so index permutations of the
+// operands and of the output (the einsum strings of the CCSD residual, e.g.
+// 'imae,mbej->ijab') are folded into address generation and never materialised.
+// This is the oracle-grade GPU path of the engine: exact FP64 products, FP64 sums.
+#include "common.cuh"
+#include <algorithm>
+
+namespace pcg {
+namespace {
+
+constexpr int BM = 64, BN = 64, BK = 16, NT = 128;
+
+struct F64Args {
+  SubIdx m, n, k;  // m: (A, C) strides; n: (B, C) strides; k: (A, B) strides
+  long long M, N, K;
+  long long k_per_split;
+  double alpha, beta;
+  const double* A;
+  const double* B;
+  double* C;
+  int a_kfast, b_kfast, atomic_out;
+};
+
+__device__ __forceinline__ void dmma(double (&c)[2], double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(c[0]), "+d"(c[1])
+               : "d"(a), "d"(b));
+}
+
+__global__ void __launch_bounds__(NT) contract_f64_kernel(const F64Args p) {
+  __shared__ double As[BK][BM + 2];
+  __shared__ double Bs[BK][BN + 2];
+  __shared__ long long aoff[BM], coffm[BM], boff[BN], coffn[BN];
+  __shared__ long long akoff[BK], bkoff[BK];
+
+  const int tid = threadIdx.x;
+  const long long m0 = (long long)blockIdx.y * BM;
+  const long long n0 = (long long)blockIdx.x * BN;
+  const long long kbeg = (long long)blockIdx.z * p.k_per_split;
+  const long long kend = min(p.K, kbeg + p.k_per_split);
+
+  if (tid < BM) {
+    long long r = m0 + tid, o0 = 0, o1 = 0;
+    if (r < p.M) sub_offsets(p.m, r, o0, o1);
+    aoff[tid] = o0;
+    coffm[tid] = o1;
+  } else {
+    int t = tid - BM;
+    long long r = n0 + t, o0 = 0, o1 = 0;
+    if (r < p.N) sub_offsets(p.n, r, o0, o1);
+    boff[t] = o0;
+    coffn[t] = o1;
+  }
+
+  const int warp = tid >> 5, lane = tid & 31;
+  const int wm = warp >> 1, wn = warp & 1;
+  const int g = lane >> 2, t4 = lane & 3;
+  double acc[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+
+  double ra[8], rb[8];
+  auto kofs = [&](long long kt) {
+    if (tid < BK) {
+      long long r = kt + tid, o0 = 0, o1 = 0;
+      if (r < kend) sub_offsets(p.k, r, o0, o1);
+      akoff[tid] = o0;
+      bkoff[tid] = o1;
+    }
+  };
+  auto load = [&](long long kt) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      int e = tid + NT * i;
+      int mm, kk;
+      if (p.a_kfast) { kk = e % BK; mm = e / BK; } else { mm = e % BM; kk = e / BM; }
+      bool ok = (m0 + mm < p.M) && (kt + kk < kend);
+      ra[i] = ok ? __ldg(p.A + aoff[mm] + akoff[kk]) : 0.0;
+      int nn;
+      if (p.b_kfast) { kk = e % BK; nn = e / BK; } else { nn = e % BN; kk = e / BN; }
+      ok = (n0 + nn < p.N) && (kt + kk < kend);
+      rb[i] = ok ? __ldg(p.B + boff[nn] + bkoff[kk]) : 0.0;
+    }
+  };
+  auto store = [&]() {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      int e = tid + NT * i;
+      int mm, kk;
+      if (p.a_kfast) { kk = e % BK; mm = e / BK; } else { mm = e % BM; kk = e / BM; }
+      As[kk][mm] = ra[i];
+      int nn;
+      if (p.b_kfast) { kk = e % BK; nn = e / BK; } else { nn = e % BN; kk = e / BN; }
+      Bs[kk][nn] = rb[i];
+    }
+  };
+
+  kofs(kbeg);
+  __syncthreads();
+  if (kbeg < kend) load(kbeg);
+  for (long long kt = kbeg; kt < kend; kt += BK) {
+    __syncthreads();  // previous compute done with As/Bs and akoff
+    store();
+    if (kt + BK < kend) kofs(kt + BK);
+    __syncthreads();
+    if (kt + BK < kend) load(kt + BK);  // global loads overlap the DMMAs below
+#pragma unroll
+    for (int ks = 0; ks < BK; ks += 4) {
+      double a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[ks + t4][wm * 32 + i * 8 + g];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[ks + t4][wn * 32 + j * 8 + g];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) dmma(acc[i][j], a[i], b[j]);
+    }
+  }
+
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    int row = wm * 32 + i * 8 + g;
+    if (m0 + row >= p.M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        int col = wn * 32 + j * 8 + 2 * t4 + h;
+        if (n0 + col >= p.N) continue;
+        double* dst = p.C + coffm[row] + coffn[col];
+        double v = p.alpha * acc[i][j][h];
+        if (p.atomic_out) {
+          atomicAdd(dst, v);
+        } else if (p.beta == 0.0) {
+          *dst = v;
+        } else {
+          *dst = p.beta * *dst + v;
+        }
+      }
+    }
+  }
+}
+
+// C[m, n] *= beta over the strided M x N range (used before a split-K accumulation).
+__global__ void scale_strided_kernel(SubIdx m, SubIdx n, long long M, long long N, double beta,
+                                     double* C) {
+  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long total = M * N;
+  for (; idx < total; idx += (long long)gridDim.x * blockDim.x) {
+    long long r = idx / N, c = idx % N, a0, a1, b0, b1;
+    sub_offsets(m, r, a0, a1);
+    sub_offsets(n, c, b0, b1);
+    double* dst = C + a1 + b1;
+    *dst = (beta == 0.0) ? 0.0 : beta * *dst;
+  }
+}
+
+bool fill_sub(SubIdx& d, int n, const long long* ext, const long long* s0, const long long* s1,
+              const char* what) {
+  if (n < 0 || n > kMaxSub) {
+    set_error("pcg_contract_f64: %s has %d sub-indices (max %d)", what, n, kMaxSub);
+    return false;
+  }
+  d.n = n;
+  for (int q = 0; q < n; ++q) {
+    if (ext[q] <= 0) {
+      set_error("pcg_contract_f64: %s extent %lld must be positive", what, ext[q]);
+      return false;
+    }
+    d.ext[q] = ext[q];
+    d.s0[q] = s0[q];
+    d.s1[q] = s1[q];
+  }
+  if (n == 0) {  // an empty group is a single index of extent 1
+    d.n = 1;
+    d.ext[0] = 1;
+    d.s0[0] = 0;
+    d.s1[0] = 0;
+  }
+  return true;
+}
+
+int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+  }
+  return sms;
+}
+
+}  // namespace
+}  // namespace pcg
+
+extern "C" int pcg_contract_f64(int m_n, const long long* m_ext, const long long* m_sa,
+                                const long long* m_sc, int n_n, const long long* n_ext,
+                                const long long* n_sb, const long long* n_sc, int k_n,
+                                const long long* k_ext, const long long* k_sa,
+                                const long long* k_sb, double alpha, const double* A,
+                                const double* B, double beta, double* C, void* stream) {
+  using namespace pcg;
+  F64Args p{};
+  if (!fill_sub(p.m, m_n, m_ext, m_sa, m_sc, "M") || !fill_sub(p.n, n_n, n_ext, n_sb, n_sc, "N") ||
+      !fill_sub(p.k, k_n, k_ext, k_sa, k_sb, "K"))
+    return -1;
+  if (!A || !B || !C) {
+    set_error("pcg_contract_f64: null operand pointer");
+    return -1;
+  }
+  p.M = sub_total(p.m);
+  p.N = sub_total(p.n);
+  p.K = sub_total(p.k);
+  p.alpha = alpha;
+  p.beta = beta;
+  p.A = A;
+  p.B = B;
+  p.C = C;
+  // Load the operand tile along whichever index is unit-stride in memory.
+  p.a_kfast = (p.k.s0[p.k.n - 1] == 1) ? 1 : 0;
+  p.b_kfast = (p.k.s1[p.k.n - 1] == 1) ? 1 : 0;
+  cudaStream_t st = (cudaStream_t)stream;
+  long long mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
+  if (mt > 65535) {
+    set_error("pcg_contract_f64: M=%lld too large", p.M);
+    return -1;
+  }
+  long long tiles = mt * nt;
+  long long target = 2LL * num_sms();
+  long long splits = 1;
+  if (tiles < target && p.K >= 8 * BK) {
+    splits = (target + tiles - 1) / tiles;
+    long long maxs = p.K / (4 * BK);
+    if (splits > maxs) splits = maxs;
+    if (splits > 64) splits = 64;
+    if (splits < 1) splits = 1;
+  }
+  long long kps = (p.K + splits - 1) / splits;
+  kps = ((kps + BK - 1) / BK) * BK;
+  splits = (p.K + kps - 1) / kps;
+  p.k_per_split = kps;
+  p.atomic_out = splits > 1;
+  if (p.atomic_out && beta != 1.0) {
+    long long total = p.M * p.N;
+    int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
+    scale_strided_kernel<<<blocks, 256, 0, st>>>(p.m, p.n, p.M, p.N, beta, C);
+    PCG_CHECK_LAUNCH("pcg_contract_f64/scale");
+  }
+  dim3 grid((unsigned)nt, (unsigned)mt, (unsigned)splits);
+  contract_f64_kernel<<<grid, NT, 0, st>>>(p);
+  PCG_CHECK_LAUNCH("pcg_contract_f64");
+  return 0;
+}

@@ -1,0 +1,313 @@
+// HBM-bound FP64 kernels of the CCSD iteration: tau builds, operand combinations, the
+// r2 symmetrisation, the Jacobi amplitude update with its norm, the energy expression and
+// the DIIS dot products / linear combinations.  All are grid-stride loops over the o^2 v^2
+// amplitude space; the reductions are two-stage (per-block partials in a caller-provided
+// work buffer, then one block) so every sum is deterministic run to run.
+#include "common.cuh"
+#include <algorithm>
+
+namespace pcg {
+namespace {
+
+constexpr int EW_THREADS = 256;
+constexpr int RED_BLOCKS = 1024;  // partials per reduced scalar
+
+int ew_blocks(long long n) {
+  long long b = (n + EW_THREADS - 1) / EW_THREADS;
+  return (int)std::max<long long>(1, std::min<long long>(b, 152LL * 16));
+}
+
+__device__ __forceinline__ double block_sum(double v) {
+  __shared__ double red[EW_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  v = (threadIdx.x < EW_THREADS / 32) ? red[threadIdx.x] : 0.0;
+  if (w == 0)
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;  // valid in thread 0
+}
+
+// out[j] = sum_b part[j * nb + b]
+__global__ void finish_sum_kernel(const double* part, int nb, int k, double* out) {
+  for (int j = 0; j < k; ++j) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += EW_THREADS) v += part[(long long)j * nb + b];
+    v = block_sum(v);
+    if (threadIdx.x == 0) out[j] = v;
+    __syncthreads();
+  }
+}
+
+__global__ void tau_kernel(const double* __restrict__ t1, const double* __restrict__ t2,
+                           long long no, long long nv, double f1, double f2,
+                           double* __restrict__ out) {
+  long long total = no * no * nv * nv;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    long long b = idx % nv, r = idx / nv;
+    long long a = r % nv;
+    r /= nv;
+    long long j = r % no, i = r / no;
+    double x = f1 * t2[idx];
+    if (f2 != 0.0) x += f2 * t1[i * nv + a] * t1[j * nv + b];
+    out[idx] = x;
+  }
+}
+
+struct Strides4 {
+  long long e[4], x[4], y[4], o[4];
+};
+
+__global__ void combine4_kernel(Strides4 s, double a, const double* __restrict__ X, double b,
+                                const double* __restrict__ Y, double* __restrict__ out) {
+  long long total = s.e[0] * s.e[1] * s.e[2] * s.e[3];
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    long long r = idx, ox = 0, oy = 0, oo = 0;
+#pragma unroll
+    for (int q = 3; q >= 0; --q) {
+      long long c = r % s.e[q];
+      r /= s.e[q];
+      ox += c * s.x[q];
+      oy += c * s.y[q];
+      oo += c * s.o[q];
+    }
+    double v = a * X[ox];
+    if (Y) v += b * Y[oy];
+    out[oo] = v;
+  }
+}
+
+__global__ void symmetrize_kernel(const double* __restrict__ h, long long no, long long nv,
+                                  double* __restrict__ out) {
+  long long total = no * no * nv * nv;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    long long b = idx % nv, r = idx / nv;
+    long long a = r % nv;
+    r /= nv;
+    long long j = r % no, i = r / no;
+    out[idx] = h[idx] + h[((j * no + i) * nv + b) * nv + a];
+  }
+}
+
+__global__ void update_kernel(double* __restrict__ t1, double* __restrict__ t2,
+                              const double* __restrict__ r1, const double* __restrict__ r2,
+                              const double* __restrict__ eps, long long no, long long nv,
+                              double* __restrict__ part) {
+  long long n1 = no * nv, total = n1 + no * no * nv * nv;
+  double acc = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    if (idx < n1) {
+      long long a = idx % nv, i = idx / nv;
+      double u = r1[idx] / (eps[i] - eps[no + a]);
+      t1[idx] += u;
+      acc += u * u;
+    } else {
+      long long q = idx - n1;
+      long long b = q % nv, r = q / nv;
+      long long a = r % nv;
+      r /= nv;
+      long long j = r % no, i = r / no;
+      double u = r2[q] / (eps[i] + eps[j] - eps[no + a] - eps[no + b]);
+      t2[q] += u;
+      acc += u * u;
+    }
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void energy_kernel(const double* __restrict__ fov, long long fs0, long long fs1,
+                              const double* __restrict__ L, Strides4 ls,
+                              const double* __restrict__ t1, const double* __restrict__ t2,
+                              long long no, long long nv, double* __restrict__ part) {
+  long long n1 = no * nv, total = n1 + no * no * nv * nv;
+  double acc = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    if (idx < n1) {
+      long long a = idx % nv, i = idx / nv;
+      acc += 2.0 * fov[i * fs0 + a * fs1] * t1[idx];
+    } else {
+      long long q = idx - n1;
+      long long b = q % nv, r = q / nv;
+      long long a = r % nv;
+      r /= nv;
+      long long j = r % no, i = r / no;
+      double tau = t2[q] + t1[i * nv + a] * t1[j * nv + b];
+      acc += tau * L[i * ls.o[0] + j * ls.o[1] + a * ls.o[2] + b * ls.o[3]];
+    }
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+constexpr int kMaxVec = 16;
+struct VecList {
+  const double* p[kMaxVec];
+  double c[kMaxVec];
+};
+
+__global__ void dots_kernel(const double* __restrict__ x, VecList ys, int k, long long n,
+                            double* __restrict__ part) {
+  double acc[kMaxVec];
+#pragma unroll
+  for (int j = 0; j < kMaxVec; ++j) acc[j] = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double xv = x[idx];
+#pragma unroll
+    for (int j = 0; j < kMaxVec; ++j)
+      if (j < k) acc[j] += xv * ys.p[j][idx];
+  }
+  for (int j = 0; j < k; ++j) {
+    double v = block_sum(acc[j]);
+    if (threadIdx.x == 0) part[(long long)j * gridDim.x + blockIdx.x] = v;
+    __syncthreads();
+  }
+}
+
+__global__ void lincomb_kernel(VecList xs, int k, long long n, double* __restrict__ out) {
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double v = 0.0;
+#pragma unroll
+    for (int j = 0; j < kMaxVec; ++j)
+      if (j < k) v += xs.c[j] * xs.p[j][idx];
+    out[idx] = v;
+  }
+}
+
+bool check_work(long long work_len, long long need, const char* who) {
+  if (work_len < need) {
+    set_error("%s: work buffer holds %lld doubles, needs %lld", who, work_len, need);
+    return false;
+  }
+  return true;
+}
+
+}  // namespace
+}  // namespace pcg
+
+using namespace pcg;
+
+extern "C" int pcg_tau_f64(const double* t1, const double* t2, long long no, long long nv,
+                           double f1, double f2, double* out, void* stream) {
+  if (!t1 || !t2 || !out || no <= 0 || nv <= 0) {
+    set_error("pcg_tau_f64: bad arguments");
+    return -1;
+  }
+  long long n = no * no * nv * nv;
+  tau_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(t1, t2, no, nv, f1, f2, out);
+  PCG_CHECK_LAUNCH("pcg_tau_f64");
+  return 0;
+}
+
+extern "C" int pcg_combine4_f64(const long long* ext, double a, const double* X,
+                                const long long* xs, double b, const double* Y,
+                                const long long* ys, double* out, const long long* os,
+                                void* stream) {
+  if (!X || !out) {
+    set_error("pcg_combine4_f64: null pointer");
+    return -1;
+  }
+  Strides4 s;
+  long long n = 1;
+  for (int q = 0; q < 4; ++q) {
+    s.e[q] = ext[q];
+    s.x[q] = xs[q];
+    s.y[q] = Y ? ys[q] : 0;
+    s.o[q] = os[q];
+    if (ext[q] <= 0) {
+      set_error("pcg_combine4_f64: extent %d is %lld", q, ext[q]);
+      return -1;
+    }
+    n *= ext[q];
+  }
+  combine4_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(s, a, X, b, Y, out);
+  PCG_CHECK_LAUNCH("pcg_combine4_f64");
+  return 0;
+}
+
+extern "C" int pcg_symmetrize_f64(const double* h, long long no, long long nv, double* out,
+                                  void* stream) {
+  if (!h || !out || h == out) {
+    set_error("pcg_symmetrize_f64: bad pointers (input and output must differ)");
+    return -1;
+  }
+  long long n = no * no * nv * nv;
+  symmetrize_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(h, no, nv, out);
+  PCG_CHECK_LAUNCH("pcg_symmetrize_f64");
+  return 0;
+}
+
+extern "C" int pcg_update_amps_f64(double* t1, double* t2, const double* r1, const double* r2,
+                                   const double* eps, long long no, long long nv, double* work,
+                                   long long work_len, double* rms2, void* stream) {
+  if (!check_work(work_len, RED_BLOCKS, "pcg_update_amps_f64")) return -1;
+  cudaStream_t st = (cudaStream_t)stream;
+  long long n = no * nv + no * no * nv * nv;
+  int nb = std::min(ew_blocks(n), RED_BLOCKS);
+  update_kernel<<<nb, EW_THREADS, 0, st>>>(t1, t2, r1, r2, eps, no, nv, work);
+  finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, 1, rms2);
+  PCG_CHECK_LAUNCH("pcg_update_amps_f64");
+  return 0;
+}
+
+extern "C" int pcg_energy_f64(const double* fov, const long long* fs, const double* L,
+                              const long long* ls, const double* t1, const double* t2,
+                              long long no, long long nv, double* work, long long work_len,
+                              double* out, void* stream) {
+  if (!check_work(work_len, RED_BLOCKS, "pcg_energy_f64")) return -1;
+  cudaStream_t st = (cudaStream_t)stream;
+  Strides4 s{};
+  for (int q = 0; q < 4; ++q) s.o[q] = ls[q];
+  long long n = no * nv + no * no * nv * nv;
+  int nb = std::min(ew_blocks(n), RED_BLOCKS);
+  energy_kernel<<<nb, EW_THREADS, 0, st>>>(fov, fs[0], fs[1], L, s, t1, t2, no, nv, work);
+  finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, 1, out);
+  PCG_CHECK_LAUNCH("pcg_energy_f64");
+  return 0;
+}
+
+extern "C" int pcg_dots_f64(const double* x, const double* const* ys, int k, long long n,
+                            double* work, long long work_len, double* out, void* stream) {
+  if (k < 1 || k > kMaxVec) {
+    set_error("pcg_dots_f64: k=%d outside [1, %d]", k, kMaxVec);
+    return -1;
+  }
+  if (!check_work(work_len, (long long)k * RED_BLOCKS, "pcg_dots_f64")) return -1;
+  cudaStream_t st = (cudaStream_t)stream;
+  VecList v{};
+  for (int j = 0; j < k; ++j) v.p[j] = ys[j];
+  int nb = std::min(ew_blocks(n), RED_BLOCKS);
+  dots_kernel<<<nb, EW_THREADS, 0, st>>>(x, v, k, n, work);
+  finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, k, out);
+  PCG_CHECK_LAUNCH("pcg_dots_f64");
+  return 0;
+}
+
+extern "C" int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n,
+                               double* out, void* stream) {
+  if (k < 1 || k > kMaxVec) {
+    set_error("pcg_lincomb_f64: k=%d outside [1, %d]", k, kMaxVec);
+    return -1;
+  }
+  VecList v{};
+  for (int j = 0; j < k; ++j) {
+    v.p[j] = xs[j];
+    v.c[j] = c[j];
+    if (xs[j] == out) {
+      set_error("pcg_lincomb_f64: output aliases input %d", j);
+      return -1;
+    }
+  }
+  lincomb_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(v, k, n, out);
+  PCG_CHECK_LAUNCH("pcg_lincomb_f64");
+  return 0;
+}

@@ -1,0 +1,236 @@
+"""Generate the golden fixtures of the RHF-CCSD path by running the reference itself.
+
+The reference (CrawfordGroup/pycc) is pure Python.  Its integral source needs psi4 and
+qcelemental, which are not installed, but the CCSD arithmetic never touches them: this
+script puts inert stand-ins for both modules into ``sys.modules``, imports ``pycc`` from
+the reference tree (``$PYCC_REF``, default ``/root/reference``), and assembles a ``CCwfn``
+with ``CCwfn.__new__`` plus the attributes that ``CCwfn.__init__`` would have set
+(``pycc/ccwfn.py:76-213``, ``pycc/wavefunction.py:293-332``), on the synthetic
+Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
+``residuals`` / ``solve_cc`` / ``t_vikings`` / ``t_tjl`` / ``cchbar`` -> ``cclambda``
+-> ``ccdensity`` and stores their outputs as ``.npz`` fixtures next to this file.
+
+Usage::
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--cfg2]
+
+Config 2 (no=20, nv=180) needs ~30 GB of host RAM and several minutes.
+"""
+from __future__ import annotations
+
+import argparse
+import io
+import contextlib
+import os
+import sys
+import time
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from pycc_gb300.synth import SyntheticFactors, CONFIGS  # noqa: E402
+
+
+def import_reference():
+    ref = os.environ.get("PYCC_REF", "/root/reference")
+    sys.dont_write_bytecode = True
+    for name in ("psi4", "qcelemental"):
+        if name not in sys.modules:
+            mod = types.ModuleType(name)
+            consts = types.SimpleNamespace(get=lambda *a, **k: 1.0,
+                                           conversion_factor=lambda *a, **k: 1.0)
+            mod.constants = consts
+            mod.core = types.SimpleNamespace()
+            sys.modules[name] = mod
+    sys.path.insert(0, ref)
+    import pycc  # noqa: F401
+    return pycc
+
+
+class _H:
+    pass
+
+
+def make_ref_ccwfn(pycc, F, ERI, L, no, nv, model="CCSD"):
+    from pycc.ccwfn import CCwfn
+    from pycc.device import DeviceManager
+    w = CCwfn.__new__(CCwfn)
+    w.model = model
+    w.method = model
+    w.orbital_basis = "spatial"
+    w.local = None
+    w.need_singles = ['CCSD', 'CCSD(T)', 'CC2', 'CC3']
+    w.make_t3_density = False
+    w.store_triples = False
+    w.real_time = False
+    w.field = False
+    w.nfzc = 0
+    w.no, w.nv, w.nmo = no, nv, no + nv
+    w.o = slice(0, no)
+    w.v = slice(no, no + nv)
+    H = _H()
+    H.F = F
+    H.eps = np.diag(F).copy()
+    H.ERI = ERI
+    H.L = L
+    w.H = H
+    w.eref = 0.0
+    mgr = DeviceManager('CPU', 'DP')
+    w.device_manager = mgr
+    w.contract = mgr.contract
+    w.precision = 'DP'
+    w.device = 'CPU'
+    w.device0 = None
+    w.device1 = None
+    w.e_conv = 1e-7
+    w.r_conv = 1e-7
+    w.maxiter = 100
+    o, v = w.o, w.v
+    eps_o, eps_v = H.eps[o], H.eps[v]
+    w.Dijab = (eps_o.reshape(-1, 1, 1, 1) + eps_o.reshape(-1, 1, 1)
+               - eps_v.reshape(-1, 1) - eps_v)
+    w.Dia = eps_o.reshape(-1, 1) - eps_v
+    w.t1 = np.zeros((no, nv))
+    w.t2 = ERI[o, o, v, v].copy() / w.Dijab
+    return w
+
+
+def probe_amplitudes(no, nv, t2_mp2, seed):
+    """A non-trivial (t1, t2) pair: every singles term of the residual is exercised."""
+    rng = np.random.default_rng(1000 + seed)
+    t1 = 0.02 * rng.standard_normal((no, nv))
+    noise = 0.01 * rng.standard_normal((no, no, nv, nv))
+    noise = noise + noise.transpose(1, 0, 3, 2)       # keep t2_ijab = t2_jiba
+    t2 = t2_mp2 + noise
+    return t1, t2
+
+
+def quiet(fn, *args, **kwargs):
+    with contextlib.redirect_stdout(io.StringIO()):
+        return fn(*args, **kwargs)
+
+
+def gen_cfg1(pycc):
+    no, nv, seed = CONFIGS[1]
+    fac = SyntheticFactors(no, nv, seed)
+    F, ERI, L = fac.hamiltonian()
+    w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
+    o, v = w.o, w.v
+    out = {"no": no, "nv": nv, "seed": seed, "B_checksum": float(np.sum(fac.B * fac.B)),
+           "eps": fac.eps}
+    # residual + intermediates at a probe point with non-zero singles
+    t1, t2 = probe_amplitudes(no, nv, w.t2, seed)
+    out["probe_t1"], out["probe_t2"] = t1, t2
+    out["tau"] = w.build_tau(t1, t2)
+    out["taut"] = w.build_tau(t1, t2, 1.0, 0.5)
+    out["Fae"] = w.build_Fae(o, v, F, L, t1, t2)
+    out["Fmi"] = w.build_Fmi(o, v, F, L, t1, t2)
+    out["Fme"] = w.build_Fme(o, v, F, L, t1)
+    out["Wmnij"] = w.build_Wmnij(o, v, ERI, t1, t2)
+    out["Wmbej"] = w.build_Wmbej(o, v, ERI, L, t1, t2)
+    out["Wmbje"] = w.build_Wmbje(o, v, ERI, t1, t2)
+    out["Zmbij"] = w.build_Zmbij(o, v, ERI, t1, t2)
+    r1, r2 = w.residuals(F, t1, t2)
+    out["r1"], out["r2"] = r1, r2
+    out["ecc_probe"] = float(w.cc_energy(o, v, F, L, t1, t2))
+    # residual at the MP2 guess
+    r1m, r2m = w.residuals(F, w.t1, w.t2)
+    out["r1_mp2"], out["r2_mp2"] = r1m, r2m
+    out["ecc_mp2"] = float(w.cc_energy(o, v, F, L, w.t1, w.t2))
+    # converged CCSD, recording every iteration's energy
+    energies = []
+    orig = w.cc_energy
+
+    def rec(*a):
+        e = orig(*a)
+        energies.append(float(e))
+        return e
+    w.cc_energy = rec
+    ecc = quiet(w.solve_cc, 1e-12, 1e-12, 100, 8, 1)
+    del w.cc_energy
+    out["ecc"] = float(ecc)
+    out["ecc_iters"] = np.array(energies)
+    out["t1"], out["t2"] = w.t1, w.t2
+    # (T): the vectorised and the Lee-Rendell drivers
+    from pycc.cctriples import t_vikings, t_tjl
+    out["et_vikings"] = float(t_vikings(w))
+    out["et_tjl"] = float(t_tjl(w))
+    # Lambda and the gradient densities
+    from pycc.cchbar import cchbar
+    from pycc.cclambda import cclambda
+    from pycc.ccdensity import ccdensity
+    hbar = quiet(cchbar, w)
+    lam = quiet(cclambda, w, hbar)
+    pseudo = quiet(lam.solve_lambda, 1e-12, 1e-12, 100, 8, 1)
+    out["lambda_pseudo"] = float(pseudo)
+    out["l1"], out["l2"] = lam.l1, lam.l2
+    dens = quiet(ccdensity, w, lam)
+    D, G = quiet(dens.gradient_densities)
+    out["D"] = np.asarray(D)
+    out["Gamma"] = np.asarray(G)
+    out["E_from_densities"] = float(np.sum(D * F) + np.sum(G * ERI))
+    np.savez_compressed(os.path.join(HERE, "cfg1.npz"), **out)
+    print("cfg1: ecc = %.15f  (T) = %.15f / %.15f  pseudo = %.15f  E(D,G) = %.15f  niter = %d"
+          % (ecc, out["et_vikings"], out["et_tjl"], pseudo, out["E_from_densities"],
+             len(energies) - 1))
+
+
+def gen_cfg2(pycc, solve=True):
+    no, nv, seed = CONFIGS[2]
+    fac = SyntheticFactors(no, nv, seed)
+    t0 = time.time()
+    F, ERI, L = fac.hamiltonian()
+    print("cfg2: integrals %.1f s" % (time.time() - t0))
+    w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
+    o, v = w.o, w.v
+    out = {"no": no, "nv": nv, "seed": seed, "B_checksum": float(np.sum(fac.B * fac.B))}
+    t1, t2 = probe_amplitudes(no, nv, w.t2, seed)
+    t0 = time.time()
+    r1, r2 = w.residuals(F, t1, t2)
+    print("cfg2: residual %.1f s" % (time.time() - t0))
+    out["r1"] = r1
+    out["r2_norm"] = float(np.linalg.norm(r2))
+    out["r2_slice_ij01"] = r2[0, 1].copy()
+    out["r2_slice_ab00"] = r2[:, :, 0, 0].copy()
+    out["r2_slice_diag"] = r2[3, 3, 10:20, 100:110].copy()
+    out["r2_rowsum"] = r2.sum(axis=(2, 3))
+    out["ecc_probe"] = float(w.cc_energy(o, v, F, L, t1, t2))
+    if solve:
+        energies = []
+        orig = w.cc_energy
+
+        def rec(*a):
+            e = orig(*a)
+            energies.append(float(e))
+            return e
+        w.cc_energy = rec
+        t0 = time.time()
+        ecc = quiet(w.solve_cc, 1e-10, 1e-10, 100, 8, 1)
+        print("cfg2: solve %.1f s, %d iterations" % (time.time() - t0, len(energies) - 1))
+        out["ecc"] = float(ecc)
+        out["ecc_iters"] = np.array(energies)
+        out["t1"] = w.t1
+        out["t2_norm"] = float(np.linalg.norm(w.t2))
+        out["t2_slice_ij01"] = w.t2[0, 1].copy()
+    np.savez_compressed(os.path.join(HERE, "cfg2.npz"), **out)
+    print("cfg2: done", out.get("ecc"))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cfg2", action="store_true")
+    ap.add_argument("--no-cfg1", action="store_true")
+    args = ap.parse_args()
+    pycc = import_reference()
+    if not args.no_cfg1:
+        gen_cfg1(pycc)
+    if args.cfg2:
+        gen_cfg2(pycc)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,64 @@
+"""The CPU oracle against fixtures produced by the reference itself (tests/golden)."""
+import numpy as np
+import pytest
+
+from oracle import ccsd as oc
+from pycc_gb300.synth import SyntheticFactors
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_generator_matches_golden(cfg1, cfg1_ham):
+    fac = cfg1_ham[0]
+    assert float(np.sum(fac.B * fac.B)) == pytest.approx(float(cfg1["B_checksum"]), rel=1e-14)
+    assert np.array_equal(fac.eps, cfg1["eps"])
+
+
+def test_intermediates_cfg1(cfg1, cfg1_ham):
+    _, F, ERI, L = cfg1_ham
+    o, v = slice(0, 5), slice(5, 24)
+    X = oc.intermediates(o, v, F, ERI, L, cfg1["probe_t1"], cfg1["probe_t2"])
+    for k, val in X.items():
+        assert rel(val, cfg1[k]) < 1e-13, k
+    assert rel(oc.build_tau(cfg1["probe_t1"], cfg1["probe_t2"]), cfg1["tau"]) < 1e-14
+    assert rel(oc.build_tau(cfg1["probe_t1"], cfg1["probe_t2"], 1.0, 0.5), cfg1["taut"]) < 1e-14
+
+
+def test_residuals_cfg1(cfg1, cfg1_ham):
+    _, F, ERI, L = cfg1_ham
+    o, v = slice(0, 5), slice(5, 24)
+    r1, r2 = oc.residuals(o, v, F, ERI, L, cfg1["probe_t1"], cfg1["probe_t2"])
+    assert rel(r1, cfg1["r1"]) < 1e-12
+    assert rel(r2, cfg1["r2"]) < 1e-12
+    t1, t2 = oc.mp2_guess(F, ERI, 5)
+    r1, r2 = oc.residuals(o, v, F, ERI, L, t1, t2)
+    assert rel(r2, cfg1["r2_mp2"]) < 1e-12
+    assert np.abs(r1 - cfg1["r1_mp2"]).max() < 1e-14
+    assert oc.cc_energy(o, v, F, L, t1, t2) == pytest.approx(float(cfg1["ecc_mp2"]), abs=1e-14)
+    assert oc.cc_energy(o, v, F, L, cfg1["probe_t1"], cfg1["probe_t2"]) == pytest.approx(
+        float(cfg1["ecc_probe"]), abs=1e-13)
+
+
+def test_solve_cc_cfg1(cfg1, cfg1_ham):
+    _, F, ERI, L = cfg1_ham
+    e, t1, t2, es = oc.solve_cc(F, ERI, L, 5, 1e-12, 1e-12)
+    assert abs(e - float(cfg1["ecc"])) < 1e-11
+    assert len(es) == len(cfg1["ecc_iters"])
+    assert np.abs(np.array(es) - cfg1["ecc_iters"]).max() < 1e-11
+    assert rel(t2, cfg1["t2"]) < 1e-9
+
+
+def test_solve_cc_raises_on_maxiter(cfg1_ham):
+    _, F, ERI, L = cfg1_ham
+    with pytest.raises(RuntimeError):
+        oc.solve_cc(F, ERI, L, 5, 1e-14, 1e-14, maxiter=3)
+
+
+@pytest.mark.slow
+def test_residuals_cfg2_golden():
+    from conftest import golden
+    g = golden("cfg2.npz")
+    fac = SyntheticFactors(20, 180, 1)
+    assert float(np.sum(fac.B * fac.B)) == pytest.approx(float(g["B_checksum"]), rel=1e-14)
