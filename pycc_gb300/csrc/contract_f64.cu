@@ -163,6 +163,38 @@ __global__ void scale_strided_kernel(SubIdx m, SubIdx n, long long M, long long 
   }
 }
 
+// Outputs with a degenerate free dimension (matrix-vector shapes such as 'nf,mnef->me'):
+// one warp per output element, a warp-wide FP64 dot over K.  HBM-bound.
+__global__ void contract_gemv_kernel(const F64Args p) {
+  const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const long long total = p.M * p.N;
+  for (long long o = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; o < total;
+       o += warps) {
+    const long long m = o / p.N, n = o % p.N;
+    long long am, cm, bn, cn;
+    sub_offsets(p.m, m, am, cm);
+    sub_offsets(p.n, n, bn, cn);
+    double acc = 0.0;
+    if (p.k.n == 1) {
+      const long long sa = p.k.s0[0], sb = p.k.s1[0];
+      for (long long k = lane; k < p.K; k += 32) acc += p.A[am + k * sa] * p.B[bn + k * sb];
+    } else {
+      for (long long k = lane; k < p.K; k += 32) {
+        long long ka, kb;
+        sub_offsets(p.k, k, ka, kb);
+        acc += p.A[am + ka] * p.B[bn + kb];
+      }
+    }
+    for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
+    if (lane == 0) {
+      double* dst = p.C + cm + cn;
+      double v = p.alpha * acc;
+      *dst = (p.beta == 0.0) ? v : p.beta * *dst + v;
+    }
+  }
+}
+
 bool fill_sub(SubIdx& d, int n, const long long* ext, const long long* s0, const long long* s1,
               const char* what) {
   if (n < 0 || n > kMaxSub) {
@@ -229,6 +261,13 @@ extern "C" int pcg_contract_f64(int m_n, const long long* m_ext, const long long
   p.a_kfast = (p.k.s0[p.k.n - 1] == 1) ? 1 : 0;
   p.b_kfast = (p.k.s1[p.k.n - 1] == 1) ? 1 : 0;
   cudaStream_t st = (cudaStream_t)stream;
+  if (p.M < 8 || p.N < 8) {
+    long long warps = p.M * p.N;
+    int blocks = (int)std::min<long long>((warps * 32 + 255) / 256, 152LL * 64);
+    contract_gemv_kernel<<<blocks, 256, 0, st>>>(p);
+    PCG_CHECK_LAUNCH("pcg_contract_f64/gemv");
+    return 0;
+  }
   long long mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
   if (mt > 65535) {
     set_error("pcg_contract_f64: M=%lld too large", p.M);

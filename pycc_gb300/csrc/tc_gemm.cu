@@ -1,0 +1,662 @@
+// Tensor-core contraction engine of the mixed-precision CCSD path (sm_103a, tcgen05).
+//
+//   C[m, n] = beta * C[m, n] + alpha * sum_k A[m, k] * B[n, k]        (C in FP64)
+//
+// * Operands are K-major row matrices in HBM ([rows][ld], K contiguous, ld a multiple of
+//   the K block), produced by the pack kernel below from any strided FP64 source
+//   (index permutations, the tau / 2t2-t2' combinations and the t1 outer products are
+//   folded into the gather, together with the precision conversion).
+// * Formats: BF16; split-BF16x3 (A = Ah + Al, B = Bh + Bl, three passes Ah.Bh + Ah.Bl +
+//   Al.Bh accumulated in the same TMEM tile); FP8 E4M3 with one FP32 scale per row of
+//   each operand (applied in the epilogue).
+// * Mainloop: one CTA computes a 128 x BN FP32 tile in TMEM.  Warp 0 lane 0 issues TMA
+//   (cp.async.bulk.tensor, 128B swizzle) into an S-stage shared-memory ring; warp 1
+//   lane 0 issues tcgen05.mma (kind::f16 or kind::f8f6f4) and releases stages with
+//   tcgen05.commit; all four warps then drain TMEM (tcgen05.ld 32x32b) and write FP64
+//   with the output permutation folded into per-row / per-column offsets.
+// * Every mbarrier wait is bounded (globaltimer); on expiry the CTA records a status code
+//   in a caller-provided device word, stops issuing work and releases its TMEM.
+#include "common.cuh"
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+#include <algorithm>
+
+namespace pcg {
+namespace tc {
+
+constexpr int BM = 128;
+constexpr int KBYTES = 128;            // bytes of K per stage row (one 128B swizzle span)
+constexpr int NT = 128;
+constexpr unsigned long long kWaitNs = 4000000000ull;  // 4 s bound on any single wait
+
+enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2 };
+
+struct EpiIdx {
+  int n;
+  long long ext[kMaxSub];
+  long long s[kMaxSub];
+};
+
+struct Args {
+  long long M, N;
+  int nkb;          // K blocks per pass in this split
+  int kb_per_split; // K blocks handled by one split (blockIdx.z)
+  int nkb_total;    // K blocks of the whole K range
+  int npass;        // 1, or 3 for split-BF16x3
+  int fp8;
+  EpiIdx em, en;
+  double alpha, beta;
+  double* C;
+  const float* a_scale;
+  const float* b_scale;
+  int atomic_out;
+  int* status;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait on an mbarrier phase; false when the time bound expired.
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  unsigned long long t0 = gtimer();
+  for (;;) {
+    for (int i = 0; i < 256; ++i)
+      if (mbar_try(bar, parity)) return true;
+    if (gtimer() - t0 > kWaitNs) return false;
+  }
+}
+__device__ __forceinline__ void tma_load_2d(const CUtensorMap* tm, uint64_t* bar, void* dst, int x,
+                                            int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+      "%4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"((unsigned long long)tm), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+// K-major operand tile, 128-byte swizzle, 8-row groups 1024 B apart (sm_100 descriptor).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+__device__ __forceinline__ void umma_f16(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_f8(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ long long epi_offset(const EpiIdx& d, long long r) {
+  long long o = 0;
+  for (int q = d.n - 1; q >= 0; --q) {
+    long long e = d.ext[q];
+    o += (r % e) * d.s[q];
+    r /= e;
+  }
+  return o;
+}
+
+template <int BN>
+struct Smem {
+  static constexpr int A_BYTES = BM * KBYTES;
+  static constexpr int B_BYTES = BN * KBYTES;
+  static constexpr int STAGE = A_BYTES + B_BYTES;
+  static constexpr int STAGES = (BN >= 256) ? 4 : (BN >= 128 ? 6 : 8);
+  static constexpr int TAIL = 1024 + BN * 8;  // barriers, tmem slot, column offsets
+  static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
+};
+
+template <int BN>
+__global__ void __launch_bounds__(NT, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
+                   const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
+                   const Args p) {
+  using L = Smem<BN>;
+  constexpr int S = L::STAGES;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw = smem_u32(smem_raw);
+  uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
+  uint8_t* sA = base;
+  uint8_t* sB = base + S * L::A_BYTES;
+  uint8_t* tail = base + S * L::STAGE;
+  uint64_t* full = reinterpret_cast<uint64_t*>(tail);
+  uint64_t* empty = full + S;
+  uint64_t* done = empty + S;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  long long* colofs = reinterpret_cast<long long*>(tail + 512);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long m0 = (long long)blockIdx.y * BM;
+  const long long n0 = (long long)blockIdx.x * BN;
+  const int kb0 = blockIdx.z * p.kb_per_split;
+  const int nkb = min(p.kb_per_split, p.nkb_total - kb0);
+  const int total = nkb * p.npass;
+  constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
+
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  for (int j = tid; j < BN; j += NT) {
+    long long c = n0 + j;
+    colofs[j] = (c < p.N) ? epi_offset(p.en, c) : -1;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0 && total > 0) {
+      // ---- TMA producer ----
+      const uint32_t bytes = L::STAGE;
+      int it = 0;
+      for (; it < total; ++it) {
+        const int s = it % S;
+        if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1)) {
+          atomicExch(p.status, kStatusTimeoutEmpty);
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        const int pass = it / nkb;
+        const int kb = kb0 + (it % nkb);
+        const CUtensorMap* ta = (pass == 2) ? &tmAl : &tmAh;
+        const CUtensorMap* tb = (pass == 1) ? &tmBl : &tmBh;
+        const int kx = kb * (p.fp8 ? 128 : 64);
+        mbar_expect_tx(&full[s], bytes);
+        tma_load_2d(ta, &full[s], sA + s * L::A_BYTES, kx, (int)m0);
+        tma_load_2d(tb, &full[s], sB + s * L::B_BYTES, kx, (int)n0);
+      }
+      if (*abort_flag) {
+        // let the copies already in flight land before the CTA releases its shared memory
+        for (int j = max(0, it - S); j < it; ++j) mbar_wait(&full[j % S], (j / S) & 1);
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer ----
+      uint32_t idesc = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+      if (!p.fp8) idesc |= (1u << 7) | (1u << 10);  // A, B = BF16 (FP8 E4M3 encodes as 0)
+      for (int it = 0; it < total; ++it) {
+        const int s = it % S;
+        if (!mbar_wait(&full[s], (it / S) & 1)) {
+          atomicExch(p.status, kStatusTimeoutFull);
+          *abort_flag = 1;
+          break;
+        }
+        if (*abort_flag) break;
+        tc_fence_after();
+        const uint64_t da = sw128_desc(smem_u32(sA + s * L::A_BYTES));
+        const uint64_t db = sw128_desc(smem_u32(sB + s * L::B_BYTES));
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per 128-byte stage row
+          const uint32_t acc = (it > 0 || k > 0) ? 1u : 0u;
+          if (p.fp8)
+            umma_f8(tmem, da + 2 * k, db + 2 * k, idesc, acc);
+          else
+            umma_f16(tmem, da + 2 * k, db + 2 * k, idesc, acc);
+        }
+        umma_commit(&empty[s]);
+      }
+      umma_commit(done);
+    }
+    __syncwarp();
+  }
+
+  // ---- epilogue: TMEM -> registers -> FP64 C ----
+  bool ok = (total > 0) ? mbar_wait(done, 0) : false;
+  if (!ok && total > 0) atomicExch(p.status, kStatusTimeoutDone);
+  __syncwarp();
+  tc_fence_after();
+  ok = ok && (*abort_flag == 0);
+  const long long row = m0 + warp * 32 + lane;
+  const bool row_ok = row < p.M;
+  const long long roff = row_ok ? epi_offset(p.em, row) : 0;
+  const double ascale = (p.fp8 && row_ok) ? (double)p.a_scale[row] : 1.0;
+  if (ok) {
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 32) {
+      uint32_t r[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
+      if (!row_ok) continue;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const long long co = colofs[c0 + j];
+        if (co < 0) continue;
+        double v = (double)__uint_as_float(r[j]) * p.alpha;
+        if (p.fp8) v *= ascale * (double)p.b_scale[n0 + c0 + j];
+        double* dst = p.C + roff + co;
+        if (p.atomic_out)
+          atomicAdd(dst, v);
+        else if (p.beta == 0.0)
+          *dst = v;
+        else
+          *dst = p.beta * *dst + v;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS));
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pack: dst[r][k] = convert(a*X + b*Y + c*P*Q) at per-source offsets rowoff_s(r)+koff_s(k).
+// ---------------------------------------------------------------------------------------
+struct PackIdx {
+  int n;
+  long long ext[kMaxSub];
+  long long s[4][kMaxSub];  // strides of sources X, Y, P, Q
+};
+
+__device__ __forceinline__ void pack_offsets(const PackIdx& d, long long r, long long (&o)[4]) {
+  o[0] = o[1] = o[2] = o[3] = 0;
+  for (int q = d.n - 1; q >= 0; --q) {
+    long long e = d.ext[q];
+    long long x = r % e;
+    r /= e;
+    o[0] += x * d.s[0][q];
+    o[1] += x * d.s[1][q];
+    o[2] += x * d.s[2][q];
+    o[3] += x * d.s[3][q];
+  }
+}
+
+struct PackArgs {
+  PackIdx r, k;
+  long long R, K, Kp;
+  double a, b, c;
+  const double* X;
+  const double* Y;
+  const double* P;
+  const double* Q;
+  void* hi;
+  void* lo;
+  float* scale;
+  int fmt;
+};
+
+__device__ __forceinline__ double pack_value(const PackArgs& p, const long long (&ro)[4],
+                                             long long k) {
+  long long ko[4];
+  pack_offsets(p.k, k, ko);
+  double v = p.X ? p.a * p.X[ro[0] + ko[0]] : 0.0;
+  if (p.Y) v += p.b * p.Y[ro[1] + ko[1]];
+  if (p.P) v += p.c * p.P[ro[2] + ko[2]] * p.Q[ro[3] + ko[3]];
+  return v;
+}
+
+// One CTA per row; BF16 / split-BF16 outputs.
+__global__ void pack_bf16_kernel(const PackArgs p) {
+  const long long r = blockIdx.x + (long long)blockIdx.y * 65535;
+  if (r >= p.R) return;
+  long long ro[4];
+  pack_offsets(p.r, r, ro);
+  __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(p.hi) + r * p.Kp;
+  __nv_bfloat16* lo = p.lo ? reinterpret_cast<__nv_bfloat16*>(p.lo) + r * p.Kp : nullptr;
+  for (long long k = threadIdx.x; k < p.Kp; k += blockDim.x) {
+    double v = (k < p.K) ? pack_value(p, ro, k) : 0.0;
+    __nv_bfloat16 h = __double2bfloat16(v);
+    hi[k] = h;
+    if (lo) lo[k] = __double2bfloat16(v - (double)__bfloat162float(h));
+  }
+}
+
+// One CTA per row; FP8 E4M3 with a per-row scale (row absmax / 448).
+__global__ void pack_fp8_kernel(const PackArgs p) {
+  const long long r = blockIdx.x + (long long)blockIdx.y * 65535;
+  if (r >= p.R) return;
+  long long ro[4];
+  pack_offsets(p.r, r, ro);
+  double m = 0.0;
+  for (long long k = threadIdx.x; k < p.K; k += blockDim.x) m = fmax(m, fabs(pack_value(p, ro, k)));
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) red[0] = m;
+  }
+  __syncthreads();
+  m = red[0];
+  const double s = (m > 0.0) ? m / 448.0 : 1.0;
+  if (threadIdx.x == 0) p.scale[r] = (float)s;
+  const double inv = 1.0 / (double)(float)s;
+  __nv_fp8_e4m3* dst = reinterpret_cast<__nv_fp8_e4m3*>(p.hi) + r * p.Kp;
+  for (long long k = threadIdx.x; k < p.Kp; k += blockDim.x) {
+    double v = (k < p.K) ? pack_value(p, ro, k) * inv : 0.0;
+    dst[k] = __nv_fp8_e4m3((float)v);
+  }
+}
+
+__global__ void scale_epi_kernel(EpiIdx em, EpiIdx en, long long M, long long N, double beta,
+                                 double* C) {
+  long long total = M * N;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    double* dst = C + epi_offset(em, idx / N) + epi_offset(en, idx % N);
+    *dst = (beta == 0.0) ? 0.0 : beta * *dst;
+  }
+}
+
+// ---- host side --------------------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* ptr = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)ptr;
+  }
+  return fn;
+}
+
+bool make_map(CUtensorMap* m, const void* base, long long rows, long long ld_bytes,
+              long long k_bytes, int elem_bytes, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) {
+    set_error("pcg_tc_gemm: cuTensorMapEncodeTiled unavailable");
+    return false;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)(k_bytes / elem_bytes), (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld_bytes};
+  cuuint32_t box[2] = {(cuuint32_t)(KBYTES / elem_bytes), (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(m, elem_bytes == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
+                  2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("pcg_tc_gemm: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return false;
+  }
+  return true;
+}
+
+int num_sms() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 148;
+  }
+  return sms;
+}
+
+template <int BN>
+int launch(const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh,
+           const CUtensorMap& bl, const Args& a, long long mt, long long nt, int splits,
+           cudaStream_t st) {
+  static bool attr = false;
+  const int smem = Smem<BN>::TOTAL;
+  if (!attr) {
+    cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    attr = true;
+  }
+  dim3 grid((unsigned)nt, (unsigned)mt, (unsigned)splits);
+  tc_gemm_kernel<BN><<<grid, NT, smem, st>>>(ah, al, bh, bl, a);
+  PCG_CHECK_LAUNCH("pcg_tc_gemm");
+  return 0;
+}
+
+bool fill_epi(EpiIdx& d, int n, const long long* ext, const long long* s, const char* what) {
+  if (n < 0 || n > kMaxSub) {
+    set_error("pcg_tc_gemm: %s has %d sub-indices (max %d)", what, n, kMaxSub);
+    return false;
+  }
+  d.n = n ? n : 1;
+  if (!n) {
+    d.ext[0] = 1;
+    d.s[0] = 0;
+  }
+  for (int q = 0; q < n; ++q) {
+    if (ext[q] <= 0) {
+      set_error("pcg_tc_gemm: %s extent must be positive", what);
+      return false;
+    }
+    d.ext[q] = ext[q];
+    d.s[q] = s[q];
+  }
+  return true;
+}
+
+bool fill_pack(PackIdx& d, int n, const long long* ext, const long long* str) {
+  if (n < 0 || n > kMaxSub) {
+    set_error("pcg_pack_operand: %d sub-indices (max %d)", n, kMaxSub);
+    return false;
+  }
+  d.n = n ? n : 1;
+  for (int q = 0; q < kMaxSub; ++q) {
+    d.ext[q] = 1;
+    for (int s = 0; s < 4; ++s) d.s[s][q] = 0;
+  }
+  for (int q = 0; q < n; ++q) {
+    if (ext[q] <= 0) {
+      set_error("pcg_pack_operand: extent must be positive");
+      return false;
+    }
+    d.ext[q] = ext[q];
+    for (int s = 0; s < 4; ++s) d.s[s][q] = str[s * kMaxSub + q];
+  }
+  return true;
+}
+
+}  // namespace tc
+}  // namespace pcg
+
+using namespace pcg;
+using namespace pcg::tc;
+
+extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* r_str,
+                                int k_n, const long long* k_ext, const long long* k_str,
+                                long long Kp, double a, const double* X, double b,
+                                const double* Y, double c, const double* P, const double* Q,
+                                void* hi, void* lo, float* row_scale, void* stream) {
+  PackArgs p{};
+  if (!fill_pack(p.r, r_n, r_ext, r_str) || !fill_pack(p.k, k_n, k_ext, k_str)) return -1;
+  if ((!X && !P) || !hi || (fmt == kBF16x3 && !lo) || (fmt == kFP8 && !row_scale) || (P && !Q) ||
+      fmt < 0 || fmt > 2) {
+    set_error("pcg_pack_operand: bad pointers for format %d", fmt);
+    return -1;
+  }
+  p.R = 1;
+  for (int q = 0; q < p.r.n; ++q) p.R *= p.r.ext[q];
+  p.K = 1;
+  for (int q = 0; q < p.k.n; ++q) p.K *= p.k.ext[q];
+  const int kblk = (fmt == kFP8) ? 128 : 64;
+  if (Kp < p.K || Kp % kblk != 0) {
+    set_error("pcg_pack_operand: Kp=%lld must be >= K=%lld and a multiple of %d", Kp, p.K, kblk);
+    return -1;
+  }
+  p.Kp = Kp;
+  p.a = a;
+  p.b = b;
+  p.c = c;
+  p.X = X;
+  p.Y = Y;
+  p.P = P;
+  p.Q = Q;
+  p.hi = hi;
+  p.lo = (fmt == kBF16x3) ? lo : nullptr;
+  p.scale = row_scale;
+  p.fmt = fmt;
+  dim3 grid((unsigned)std::min<long long>(p.R, 65535), (unsigned)((p.R + 65534) / 65535));
+  cudaStream_t st = (cudaStream_t)stream;
+  if (fmt == kFP8)
+    pack_fp8_kernel<<<grid, 256, 0, st>>>(p);
+  else
+    pack_bf16_kernel<<<grid, 256, 0, st>>>(p);
+  PCG_CHECK_LAUNCH("pcg_pack_operand");
+  return 0;
+}
+
+extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_lo, long long M,
+                           long long lda, const void* B_hi, const void* B_lo, long long N,
+                           long long ldb, long long Kp, const float* a_scale,
+                           const float* b_scale, int m_n, const long long* m_ext,
+                           const long long* m_sc, int n_n, const long long* n_ext,
+                           const long long* n_sc, double alpha, double beta, double* C,
+                           int* status, void* stream) {
+  if (fmt < 0 || fmt > 2) {
+    set_error("pcg_tc_gemm: unknown format %d", fmt);
+    return -1;
+  }
+  const int eb = (fmt == kFP8) ? 1 : 2;
+  const int kblk = KBYTES / eb;
+  if (!A_hi || !B_hi || !C || !status || (fmt == kBF16x3 && (!A_lo || !B_lo)) ||
+      (fmt == kFP8 && (!a_scale || !b_scale))) {
+    set_error("pcg_tc_gemm: null pointer for format %d", fmt);
+    return -1;
+  }
+  if (M <= 0 || N <= 0 || Kp <= 0 || Kp % kblk != 0 || lda < Kp || ldb < Kp ||
+      (lda * eb) % 16 != 0 || (ldb * eb) % 16 != 0) {
+    set_error("pcg_tc_gemm: bad sizes M=%lld N=%lld Kp=%lld lda=%lld ldb=%lld", M, N, Kp, lda, ldb);
+    return -1;
+  }
+  const void* ptrs[4] = {A_hi, A_lo, B_hi, B_lo};
+  for (const void* q : ptrs)
+    if (q && ((uintptr_t)q % 16) != 0) {
+      set_error("pcg_tc_gemm: operand base not 16-byte aligned");
+      return -1;
+    }
+  if (M > 0x7fffffffLL - BM || N > 0x7fffffffLL) {
+    set_error("pcg_tc_gemm: M or N exceeds the TMA coordinate range");
+    return -1;
+  }
+  Args a{};
+  a.M = M;
+  a.N = N;
+  a.fp8 = (fmt == kFP8);
+  a.npass = (fmt == kBF16x3) ? 3 : 1;
+  if (!fill_epi(a.em, m_n, m_ext, m_sc, "M") || !fill_epi(a.en, n_n, n_ext, n_sc, "N")) return -1;
+  a.alpha = alpha;
+  a.beta = beta;
+  a.C = C;
+  a.a_scale = a_scale;
+  a.b_scale = b_scale;
+  a.status = status;
+  const int BN = (N <= 64) ? 64 : (N <= 128 ? 128 : 256);
+  long long mt = (M + BM - 1) / BM, nt = (N + BN - 1) / BN;
+  if (mt > 65535 || nt > 0x7fffffffLL) {
+    set_error("pcg_tc_gemm: grid too large (M tiles %lld)", mt);
+    return -1;
+  }
+  const int nkb = (int)(Kp / kblk);
+  long long tiles = mt * nt;
+  int splits = 1;
+  const int sms = num_sms();
+  if (tiles < sms && nkb >= 8) {
+    splits = (int)std::min<long long>((sms + tiles - 1) / tiles, nkb / 4);
+    splits = std::max(1, std::min(splits, 64));
+  }
+  int kps = (nkb + splits - 1) / splits;
+  splits = (nkb + kps - 1) / kps;
+  a.nkb_total = nkb;
+  a.kb_per_split = kps;
+  a.atomic_out = splits > 1;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a.atomic_out && beta != 1.0) {
+    int blocks = (int)std::min<long long>((M * N + 255) / 256, 4096);
+    scale_epi_kernel<<<blocks, 256, 0, st>>>(a.em, a.en, M, N, beta, C);
+    PCG_CHECK_LAUNCH("pcg_tc_gemm/scale");
+  }
+  CUtensorMap ah, al, bh, bl;
+  if (!make_map(&ah, A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
+  if (!make_map(&al, A_lo ? A_lo : A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
+  if (!make_map(&bh, B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
+  if (!make_map(&bl, B_lo ? B_lo : B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
+  switch (BN) {
+    case 64: return launch<64>(ah, al, bh, bl, a, mt, nt, splits, st);
+    case 128: return launch<128>(ah, al, bh, bl, a, mt, nt, splits, st);
+    default: return launch<256>(ah, al, bh, bl, a, mt, nt, splits, st);
+  }
+}

@@ -1,0 +1,200 @@
+"""Mixed-precision RHF-CCSD residual on the tcgen05 tensor-core engine.
+
+The same equations as ``CCwfn.residuals`` (``pycc/ccwfn.py:321-945``), with every
+contraction of O(o^2 v^3) cost or more issued to the tensor cores (``pycc_gb300.tc``):
+
+* fast mode: BF16 operands, FP32 accumulation in TMEM; the <ab|ef> ladder in FP8 E4M3
+  with per-row scales when ``vvvv_fp8`` is set;
+* final mode (update norm below ``switch_threshold``, or ``precision='SP'``): compensated
+  split-BF16x3 products everywhere.
+
+Amplitudes, intermediates, residuals, denominators, the energy, the update norm and DIIS stay
+FP64 (the GEMM epilogue accumulates into FP64).  Matrix-vector shaped and O(o^2 v^2) terms
+run on the FP64 kernels.  Two algebraically exact refactorings are shared with the FP64 path:
+the t1 t1 <mb|ej> / <ma|je> terms of r2 are evaluated in two O(o^3 v^2) steps instead of one
+O(o^3 v^3) step, and the Fme dressings of Fae / Fmi are folded into the dressed
+one-body matrices before they multiply t2.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from .contract import contract_f64
+from .tc import FMT_BF16, FMT_BF16X3, FMT_FP8, Operand, TCEngine
+
+
+class MixedResidual:
+    def __init__(self, w, mode="auto"):
+        self.w = w
+        self.tc = TCEngine(w.device1, w.stream)
+        self.fixed_final = mode == "bf16x3"
+        self.final = self.fixed_final
+        self.history = []
+
+    # -- precision schedule ---------------------------------------------------------------
+    def select_mode(self, rms):
+        if not self.fixed_final and rms < self.w.switch_threshold:
+            self.final = True
+        self.history.append(self.mode_name())
+
+    def force_final(self):
+        self.final = True
+
+    def is_final_mode(self):
+        return self.final
+
+    def mode_name(self):
+        if self.final:
+            return "bf16x3"
+        return "bf16+fp8" if self.w.vvvv_fp8 else "bf16"
+
+    def fmt(self):
+        return FMT_BF16X3 if self.final else FMT_BF16
+
+    def ladder_fmt(self):
+        if self.final:
+            return FMT_BF16X3
+        return FMT_FP8 if self.w.vvvv_fp8 else FMT_BF16
+
+    # -- helpers --------------------------------------------------------------------------
+    def tcc(self, subs, A, B, out, alpha=1.0, beta=1.0, fmt=None):
+        return self.tc.contract(subs, A, B, out, alpha=alpha, beta=beta,
+                                fmt=self.fmt() if fmt is None else fmt)
+
+    def eri(self, pat, labels):
+        return Operand.of(labels, self.w.H.ERI.blocks[pat], key=("ERI", pat))
+
+    def ll(self, pat, labels):
+        return Operand.of(labels, self.w.H.L.blocks[pat], key=("L", pat))
+
+    @staticmethod
+    def t2op(labels, t2, t2lab=None):
+        return Operand.of(labels, t2) if t2lab is None else Operand(labels, (t2, t2lab))
+
+    # -- intermediates (pycc/ccwfn.py:458-715) -------------------------------------------
+    def build_Fae(self, F, t1, t2):
+        o, v = self.w.o, self.w.v
+        Fae = F[v, v].clone()
+        contract_f64('me,ma->ae', F[o, v], t1, out=Fae, alpha=-0.5, beta=1.0)
+        contract_f64('mf,mafe->ae', t1, self.w.H.L[o, v, v, v], out=Fae, beta=1.0)
+        taut = Operand('mnaf', (t2, 'mnaf'), P=(t1, 'ma'), Q=(t1, 'nf'), c=0.5)
+        self.tcc('mnaf,mnef->ae', taut, self.ll('oovv', 'mnef'), Fae, alpha=-1.0)
+        return Fae
+
+    def build_Fmi(self, F, t1, t2):
+        o, v = self.w.o, self.w.v
+        Fmi = F[o, o].clone()
+        contract_f64('ie,me->mi', t1, F[o, v], out=Fmi, alpha=0.5, beta=1.0)
+        contract_f64('ne,mnie->mi', t1, self.w.H.L[o, o, o, v], out=Fmi, beta=1.0)
+        taut = Operand('inef', (t2, 'inef'), P=(t1, 'ie'), Q=(t1, 'nf'), c=0.5)
+        self.tcc('inef,mnef->mi', taut, self.ll('oovv', 'mnef'), Fmi)
+        return Fmi
+
+    def build_Fme(self, F, t1):
+        o, v = self.w.o, self.w.v
+        Fme = F[o, v].clone()
+        contract_f64('nf,mnef->me', t1, self.w.H.L[o, o, v, v], out=Fme, beta=1.0)
+        return Fme
+
+    def build_Wmnij(self, t1, t2):
+        o = self.w.o
+        W = self.w.H.ERI[o, o, o, o].clone()
+        self.tcc('je,mnie->mnij', Operand.of('je', t1), self.eri('ooov', 'mnie'), W)
+        self.tcc('ie,mnej->mnij', Operand.of('ie', t1), self.eri('oovo', 'mnej'), W)
+        tau = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
+        self.tcc('ijef,mnef->mnij', tau, self.eri('oovv', 'mnef'), W)
+        return W
+
+    def build_Wmbej(self, t1, t2):
+        o, v = self.w.o, self.w.v
+        W = self.w.H.ERI[o, v, v, o].clone()
+        self.tcc('jf,mbef->mbej', Operand.of('jf', t1), self.eri('ovvv', 'mbef'), W)
+        self.tcc('nb,mnej->mbej', Operand.of('nb', t1), self.eri('oovo', 'mnej'), W, alpha=-1.0)
+        X = Operand('jnfb', (t2, 'jnfb'), a=0.5, P=(t1, 'jf'), Q=(t1, 'nb'), c=1.0)
+        self.tcc('jnfb,mnef->mbej', X, self.eri('oovv', 'mnef'), W, alpha=-1.0)
+        self.tcc('njfb,mnef->mbej', Operand.of('njfb', t2), self.ll('oovv', 'mnef'), W, alpha=0.5)
+        return W
+
+    def build_Wmbje(self, t1, t2):
+        o, v = self.w.o, self.w.v
+        W = self.w._combine(-1.0, self.w.H.ERI[o, v, o, v], 0.0, None, None)
+        self.tcc('jf,mbfe->mbje', Operand.of('jf', t1), self.eri('ovvv', 'mbfe'), W, alpha=-1.0)
+        self.tcc('nb,mnje->mbje', Operand.of('nb', t1), self.eri('ooov', 'mnje'), W)
+        X = Operand('jnfb', (t2, 'jnfb'), a=0.5, P=(t1, 'jf'), Q=(t1, 'nb'), c=1.0)
+        self.tcc('jnfb,mnfe->mbje', X, self.eri('oovv', 'mnfe'), W)
+        return W
+
+    def build_Zmbij(self, t1, t2):
+        no, nv = self.w.no, self.w.nv
+        Z = torch.empty((no, nv, no, no), dtype=torch.float64, device=t2.device)
+        tau = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
+        self.tcc('mbef,ijef->mbij', self.eri('ovvv', 'mbef'), tau, Z, beta=0.0)
+        return Z
+
+    # -- residuals (pycc/ccwfn.py:718-945) ------------------------------------------------
+    def r_T1(self, F, t1, t2, Fae, Fme, Fmi):
+        o, v = self.w.o, self.w.v
+        r = F[v, o].transpose(0, 1).contiguous()
+        contract_f64('ie,ae->ia', t1, Fae, out=r, beta=1.0)
+        contract_f64('mi,ma->ia', Fmi, t1, out=r, alpha=-1.0, beta=1.0)
+        t2s = Operand('imae', (t2, 'imae'), a=2.0, Y=(t2, 'imea'), b=-1.0)
+        self.tcc('imae,me->ia', t2s, Operand.of('me', Fme), r)
+        contract_f64('nf,nafi->ia', t1, self.w.H.L[o, v, v, o], out=r, beta=1.0)
+        t2s = Operand('mief', (t2, 'mief'), a=2.0, Y=(t2, 'mife'), b=-1.0)
+        self.tcc('mief,maef->ia', t2s, self.eri('ovvv', 'maef'), r)
+        self.tcc('mnae,nmei->ia', Operand.of('mnae', t2), self.ll('oovo', 'nmei'), r, alpha=-1.0)
+        return r
+
+    def r_T2_half(self, F, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij):
+        o, v = self.w.o, self.w.v
+        no, nv = self.w.no, self.w.nv
+        ERI = self.w.H.ERI
+        r = self.w._combine(0.5, ERI[v, v, o, o].permute(2, 3, 0, 1), 0.0, None, None)
+        # t2_ijae (F_be - 1/2 t_mb F_me) and - t2_imab (F_mj + 1/2 t_je F_me)
+        Fbe = Fae.clone()
+        contract_f64('mb,me->be', t1, Fme, out=Fbe, alpha=-0.5, beta=1.0)
+        self.tcc('ijae,be->ijab', Operand.of('ijae', t2), Operand.of('be', Fbe), r)
+        Fmj = Fmi.clone()
+        contract_f64('je,me->mj', t1, Fme, out=Fmj, alpha=0.5, beta=1.0)
+        self.tcc('imab,mj->ijab', Operand.of('imab', t2), Operand.of('mj', Fmj), r, alpha=-1.0)
+        # ladders
+        tau_mn = Operand('mnab', (t2, 'mnab'), P=(t1, 'ma'), Q=(t1, 'nb'), c=1.0)
+        self.tcc('mnab,mnij->ijab', tau_mn, Operand.of('mnij', Wmnij), r, alpha=0.5)
+        tau_ij = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
+        self.tcc('ijef,abef->ijab', tau_ij, self.eri('vvvv', 'abef'), r, alpha=0.5,
+                 fmt=self.ladder_fmt())
+        self.tcc('ma,mbij->ijab', Operand.of('ma', t1), Operand.of('mbij', Zmbij), r, alpha=-1.0)
+        # rings
+        self.tcc('imae,mbej->ijab', Operand('imae', (t2, 'imae'), Y=(t2, 'imea'), b=-1.0),
+                 Operand.of('mbej', Wmbej), r)
+        self.tcc('imae,mbej->ijab', Operand.of('imae', t2),
+                 Operand('mbej', (Wmbej, 'mbej'), Y=(Wmbje, 'mbje'), b=1.0), r)
+        self.tcc('mjae,mbie->ijab', Operand.of('mjae', t2), Operand.of('mbie', Wmbje), r)
+        # - t_ie t_ma <mb|ej> - t_ie t_mb <ma|je>, two O(o^3 v^2) steps each
+        Y1 = torch.empty((no, no, nv, no), dtype=torch.float64, device=t2.device)
+        self.tcc('ie,mbej->imbj', Operand.of('ie', t1), self.eri('ovvo', 'mbej'), Y1, beta=0.0)
+        self.tcc('ma,imbj->ijab', Operand.of('ma', t1), Operand.of('imbj', Y1), r, alpha=-1.0)
+        Y2 = torch.empty((no, no, nv, no), dtype=torch.float64, device=t2.device)
+        self.tcc('ie,maje->imaj', Operand.of('ie', t1), self.eri('ovov', 'maje'), Y2, beta=0.0)
+        self.tcc('mb,imaj->ijab', Operand.of('mb', t1), Operand.of('imaj', Y2), r, alpha=-1.0)
+        self.tcc('ie,abej->ijab', Operand.of('ie', t1), self.eri('vvvo', 'abej'), r)
+        self.tcc('ma,mbij->ijab', Operand.of('ma', t1), self.eri('ovoo', 'mbij'), r, alpha=-1.0)
+        return r
+
+    def residuals(self, F, t1, t2):
+        t1 = t1.contiguous()
+        t2 = t2.contiguous()
+        Fae = self.build_Fae(F, t1, t2)
+        Fmi = self.build_Fmi(F, t1, t2)
+        Fme = self.build_Fme(F, t1)
+        Wmnij = self.build_Wmnij(t1, t2)
+        Wmbej = self.build_Wmbej(t1, t2)
+        Wmbje = self.build_Wmbje(t1, t2)
+        Zmbij = self.build_Zmbij(t1, t2)
+        r1 = self.r_T1(F, t1, t2, Fae, Fme, Fmi)
+        half = self.r_T2_half(F, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij)
+        r2 = torch.empty_like(half)
+        _lib.call("pcg_symmetrize_f64", half.data_ptr(), self.w.no, self.w.nv, r2.data_ptr(),
+                  _lib.stream_handle(self.w.stream))
+        return r1, r2

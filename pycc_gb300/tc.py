@@ -1,0 +1,220 @@
+"""Host side of the tcgen05 tensor-core contraction engine (``pcg_pack_operand`` + ``pcg_tc_gemm``).
+
+A contraction ``out = beta*out + alpha * einsum('A,B->C', opA, opB)`` is executed as
+
+1. pack: each operand is gathered from its FP64 source(s) into a K-major row matrix
+   ``[rows][Kp]`` in the GEMM's input format (BF16, BF16 hi+lo pair, or FP8 E4M3 with a
+   per-row scale).  An operand may be a combination ``a*X + b*Y + c*P*Q`` of strided FP64
+   tensors (e.g. ``2 t2 - t2.swapaxes(2,3)`` or ``t2 + t1 (x) t1``), so the
+   combinations, index permutations and the conversion happen in one pass;
+2. GEMM: 128 x BN tiles on tcgen05 with TMEM accumulators; the epilogue writes FP64 with
+   the output permutation expressed as per-row / per-column offsets.
+
+Packed operands of static tensors (the integral blocks) are cached by the caller.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+
+from . import _lib
+
+FMT_BF16, FMT_BF16X3, FMT_FP8 = 0, 1, 2
+MAX_SUB = 4
+
+
+class Operand:
+    """``a*X + b*Y + c*P*Q`` over the index labels ``labels``.
+
+    Each component is ``(tensor, labels)``; labels of the operand a component lacks are
+    broadcast (stride 0).
+    """
+
+    def __init__(self, labels, X, a=1.0, Y=None, b=0.0, P=None, Q=None, c=0.0, key=None):
+        self.labels = labels
+        self.a, self.b, self.c = a, b, c
+        self.X, self.Y, self.P, self.Q = X, Y, P, Q
+        self.key = key            # cache key for static operands (None = dynamic)
+
+    @staticmethod
+    def of(labels, t, key=None):
+        return Operand(labels, (t, labels), key=key)
+
+    def sources(self):
+        return [self.X, self.Y, self.P, self.Q]
+
+    def extents(self):
+        ext = {}
+        for s in self.sources():
+            if s is None:
+                continue
+            t, lab = s
+            for c, n in zip(lab, t.shape):
+                if ext.setdefault(c, n) != n:
+                    raise ValueError("operand index %r has extents %d and %d" % (c, ext[c], n))
+        return ext
+
+    def strides(self, label):
+        out = []
+        for s in self.sources():
+            if s is None:
+                out.append(0)
+                continue
+            t, lab = s
+            out.append(t.stride(lab.index(label)) if label in lab else 0)
+        return out
+
+    def device(self):
+        return self.X[0].device
+
+
+def _merge_multi(groups):
+    """Merge consecutive (ext, [strides...]) groups contiguous in every stride set."""
+    groups = [g for g in groups if g[0] != 1]
+    out = []
+    for e, s in groups:
+        if out:
+            pe, ps = out[-1]
+            if all(p == e * q for p, q in zip(ps, s)):
+                out[-1] = (pe * e, list(s))
+                continue
+        out.append((e, list(s)))
+    return out
+
+
+def _ptr(s):
+    return s[0].data_ptr() if s is not None else None
+
+
+class Packed:
+    """A packed K-major operand: ``hi`` (and ``lo`` / ``scale``) of shape [rows, Kp]."""
+
+    def __init__(self, fmt, rows, Kp, hi, lo=None, scale=None):
+        self.fmt, self.rows, self.Kp = fmt, rows, Kp
+        self.hi, self.lo, self.scale = hi, lo, scale
+
+    def nbytes(self):
+        return sum(t.numel() * t.element_size() for t in (self.hi, self.lo, self.scale) if t is not None)
+
+
+def kblock(fmt):
+    return 128 if fmt == FMT_FP8 else 64
+
+
+def pack(op: Operand, row_labels, k_labels, fmt, stream=None) -> Packed:
+    ext = op.extents()
+    rows = [(ext[c], op.strides(c)) for c in row_labels]
+    ks = [(ext[c], op.strides(c)) for c in k_labels]
+    R = math.prod(ext[c] for c in row_labels)
+    K = math.prod(ext[c] for c in k_labels)
+    rows, ks = _merge_multi(rows), _merge_multi(ks)
+    if len(rows) > MAX_SUB or len(ks) > MAX_SUB:
+        raise ValueError("pack: more than %d sub-indices" % MAX_SUB)
+    kb = kblock(fmt)
+    Kp = ((K + kb - 1) // kb) * kb
+    dev = op.device()
+    if fmt == FMT_FP8:
+        hi = torch.empty((R, Kp), dtype=torch.uint8, device=dev)
+        lo = None
+        scale = torch.empty(R, dtype=torch.float32, device=dev)
+    else:
+        hi = torch.empty((R, Kp), dtype=torch.bfloat16, device=dev)
+        lo = torch.empty_like(hi) if fmt == FMT_BF16X3 else None
+        scale = None
+
+    def flat(groups):
+        e = [g[0] for g in groups]
+        st = [0] * (4 * MAX_SUB)
+        for q, (_, s) in enumerate(groups):
+            for src in range(4):
+                st[src * MAX_SUB + q] = s[src]
+        return len(groups), _lib.i64s(e), _lib.i64s(st)
+
+    rn, re_, rs = flat(rows)
+    kn, ke, kst = flat(ks)
+    _lib.call("pcg_pack_operand", int(fmt), rn, re_, rs, kn, ke, kst, Kp,
+              float(op.a), _ptr(op.X), float(op.b), _ptr(op.Y), float(op.c), _ptr(op.P),
+              _ptr(op.Q), hi.data_ptr(), lo.data_ptr() if lo is not None else None,
+              scale.data_ptr() if scale is not None else None, _lib.stream_handle(stream))
+    return Packed(fmt, R, Kp, hi, lo, scale)
+
+
+def gemm(fmt, A: Packed, B: Packed, out, row_labels, col_labels, out_labels, alpha=1.0,
+         beta=1.0, status=None, stream=None):
+    """out = beta*out + alpha * A . B^T with rows/cols mapped to ``out`` through labels."""
+    if A.Kp != B.Kp:
+        raise ValueError("gemm: K mismatch %d vs %d" % (A.Kp, B.Kp))
+    ost = dict(zip(out_labels, out.stride()))
+    oext = dict(zip(out_labels, out.shape))
+    mg = _merge_multi([(oext[c], [ost[c]]) for c in row_labels])
+    ng = _merge_multi([(oext[c], [ost[c]]) for c in col_labels])
+    if len(mg) > MAX_SUB or len(ng) > MAX_SUB:
+        raise ValueError("gemm: more than %d output sub-indices" % MAX_SUB)
+    i64 = _lib.i64s
+    _lib.call("pcg_tc_gemm", int(fmt), A.hi.data_ptr(), A.lo.data_ptr() if A.lo is not None else None,
+              A.rows, A.Kp, B.hi.data_ptr(), B.lo.data_ptr() if B.lo is not None else None,
+              B.rows, B.Kp, A.Kp,
+              A.scale.data_ptr() if A.scale is not None else None,
+              B.scale.data_ptr() if B.scale is not None else None,
+              len(mg), i64([g[0] for g in mg]), i64([g[1][0] for g in mg]),
+              len(ng), i64([g[0] for g in ng]), i64([g[1][0] for g in ng]),
+              float(alpha), float(beta), out.data_ptr(), status.data_ptr(),
+              _lib.stream_handle(stream))
+
+
+class TCEngine:
+    """Plans and runs einsum-style contractions on the tensor-core engine."""
+
+    def __init__(self, device, stream=None):
+        self.device = device
+        self.stream = stream
+        self.status = torch.zeros(4, dtype=torch.int32, device=device)
+        self.cache = {}
+
+    def cached_bytes(self):
+        return sum(p.nbytes() for p in self.cache.values())
+
+    def contract(self, subscripts, A: Operand, B: Operand, out, alpha=1.0, beta=1.0, fmt=FMT_BF16):
+        lhs, rhs = subscripts.replace(" ", "").split("->")
+        la, lb = lhs.split(",")
+        if la != A.labels or lb != B.labels:
+            raise ValueError("contract: operand labels %s,%s do not match %s" % (A.labels, B.labels, lhs))
+        ost = dict(zip(rhs, out.stride()))
+        ea, eb = A.extents(), B.extents()
+        ma = [c for c in rhs if c in la and c not in lb]
+        nb = [c for c in rhs if c in lb and c not in la]
+        kk = [c for c in la if c in lb and c not in rhs]
+        if len(ma) + len(nb) != len(rhs):
+            raise ValueError("contract: batch indices are not supported (%s)" % subscripts)
+        # rows / cols in output-stride order (innermost last); K by the dynamic operand
+        ma.sort(key=lambda c: -ost[c])
+        nb.sort(key=lambda c: -ost[c])
+        dyn = A if A.key is None else B
+        dst = {c: max(abs(s) for s in dyn.strides(c)) for c in kk}
+        kk.sort(key=lambda c: -dst[c])
+        mA = math.prod(ea[c] for c in ma) if ma else 1
+        nB = math.prod(eb[c] for c in nb) if nb else 1
+        # the larger free dimension takes the 128-row tile side
+        if nB > mA:
+            A, B, ma, nb = B, A, nb, ma
+        pa = self._pack(A, ma, kk, fmt, "A")
+        pb = self._pack(B, nb, kk, fmt, "B")
+        gemm(fmt, pa, pb, out, ma, nb, rhs, alpha=alpha, beta=beta, status=self.status,
+             stream=self.stream)
+        return out
+
+    def _pack(self, op, rows, ks, fmt, side):
+        if op.key is None:
+            return pack(op, rows, ks, fmt, self.stream)
+        key = (op.key, tuple(rows), tuple(ks), fmt)
+        p = self.cache.get(key)
+        if p is None:
+            p = pack(op, rows, ks, fmt, self.stream)
+            self.cache[key] = p
+        return p
+
+    def check_status(self):
+        s = self.status.cpu()
+        if int(s.abs().sum()) != 0:
+            raise _lib.EngineError("tensor-core kernel reported a wait timeout (status %s)" % s.tolist())
