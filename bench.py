@@ -1,10 +1,19 @@
 """Benchmark of the GB300 RHF-CCSD amplitude engine.
 
-Metric: CCSD seconds per iteration and TFLOP/s at no=40, nv=300 (synthetic Hamiltonian,
-seed 2), mixed precision vs plain FP64 on one GB300.  A "step" is one full CCSD iteration
-of ``solve_cc`` (residual + Jacobi update + energy + DIIS) on device-resident amplitudes and
-integrals.  TFLOP/s uses the pinned per-iteration count of the reference formulation,
-F_iter = 2 o^2 v^4 + 18 o^3 v^3 + 10 o^2 v^3 + 4 o^4 v^2.
+Metric: CCSD TFLOP/s and seconds per iteration at no=40, nv=300 (synthetic Hamiltonian,
+seed 2, matched coupling), mixed precision vs plain FP64 on one GB300.
+
+* A step is one CCSD iteration of ``solve_cc`` (residual + Jacobi update + energy + DIIS) on
+  HBM-resident integrals and amplitudes, following the mixed engine's precision ladder
+  (FP8 ladder + BF16 -> BF16 -> split-BF16x3) from the MP2 guess: W warm-up iterations,
+  then K timed iterations.  The integral blocks (tens of GB) exceed L2 every iteration.
+* TFLOP/s uses the pinned per-iteration count of the reference formulation,
+  F_iter = 2 o^2 v^4 + 18 o^3 v^3 + 10 o^2 v^3 + 4 o^4 v^2 (counted once for every mode).
+* ``fp64``: the plain FP64 GPU form (DMMA kernels) timed over one iteration at the same size.
+* ``e2e``: ``CCwfn.residuals`` through the public API with t1/t2 copied from pinned host
+  memory and r1/r2 copied back every step.
+* ``roofline``: the <ab|ef> ladder GEMM (the dominant kernel), CUDA events on its stream.
+* ``cpu_baseline``: the CPU oracle's CCSD iteration on the host cores (bounded sample).
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -12,6 +21,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -22,10 +32,22 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "CCSD s/iter & TFLOP/s (no=40,nv=300): mixed vs FP64 on GB300 at 1e-6 Eh"
+FP64_REF = os.path.join(ROOT, "tests", "golden", "fp64_reference.json")
 
 
 def f_iter(o, v):
     return 2 * o**2 * v**4 + 18 * o**3 * v**3 + 10 * o**2 * v**3 + 4 * o**4 * v**2
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "bf16": d["bf16_tflops"],
+                "bf16_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16": 1900.0, "bf16_sustained": 1700.0, "source": "fallback"}
 
 
 class ClockSampler:
@@ -47,7 +69,8 @@ class ClockSampler:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.th = threading.Thread(target=self._read, daemon=True)
             self.th.start()
-        except (OSError, FileNotFoundError):
+            time.sleep(0.3)
+        except OSError:
             self.proc = None
 
     def _read(self):
@@ -62,40 +85,40 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, mx, reasons = [], [], set()
+        sm, mx, pw, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in self.rows:
             try:
                 sm.append(float(r[0]))
                 mx.append(float(r[1]))
+                pw.append(float(r[2]))
             except (ValueError, IndexError):
                 continue
             for name, val in zip(names, r[3:7]):
                 if val.lower() == "active":
                     reasons.add(name)
         sm.sort()
-        med = sm[len(sm) // 2] if sm else None
-        return {"sm_mhz": med, "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def cpu_reference(args, world, rank):
-    """The reference arm: the oracle port's CCSD iteration on the host cores."""
-    import numpy as np
-    if rank != 0:
-        return None
+def cpu_oracle_iteration(steps, warmup):
+    """The CPU oracle's CCSD iteration (residual + update + energy + DIIS) on the host cores.
+
+    Bounded sample: no=20, nv=180 (the no=40, nv=300 host layout of the reference needs
+    ~214 GB); TFLOP/s is reported with the same pinned flop formula at that size.
+    """
     from oracle import ccsd as oc
     from pycc_gb300.synth import SyntheticFactors
-    ncores = os.cpu_count() or 1
     o_s, v_s, seed = 20, 180, 1
-    fac = SyntheticFactors(o_s, v_s, seed)
+    fac = SyntheticFactors(o_s, v_s, seed, coupling="matched")
     F, ERI, L = fac.hamiltonian()
     o, v = slice(0, o_s), slice(o_s, o_s + v_s)
     t1, t2 = oc.mp2_guess(F, ERI, o_s)
@@ -110,94 +133,233 @@ def cpu_reference(args, world, rank):
         diis.add_error_vector(t1, t2)
         return diis.extrapolate(t1, t2)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         t1, t2 = step(t1, t2)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         t1, t2 = step(t1, t2)
-    dt = (time.perf_counter() - t0) / args.steps
-    tf = f_iter(o_s, v_s) / dt / 1e12
-    return dt, tf, ncores, "oracle CCSD iteration at no=%d,nv=%d (seed %d), %d threads" % (
-        o_s, v_s, seed, ncores)
+    dt = (time.perf_counter() - t0) / steps
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"s_per_iter": dt, "tflops": f_iter(o_s, v_s) / dt / 1e12, "cores": threads,
+            "sample": "oracle CCSD iteration (numpy/BLAS) at no=%d,nv=%d seed %d, %d steps after "
+                      "%d warm-up; %d BLAS threads" % (o_s, v_s, seed, steps, warmup, threads)}
+
+
+def reference_arm(args, rank):
+    if rank != 0:
+        return
+    res = cpu_oracle_iteration(args.steps if args.steps <= 3 else 2, min(args.warmup, 1))
+    tf = res["tflops"]
+    line = {"metric": METRIC, "value": tf, "unit": "TFLOP/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["s_per_iter"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": "RHF-CCSD iteration, synthetic Hamiltonian (CPU sample)",
+                       "no": 20, "nv": 180, "seed": 1, "coupling": "matched"},
+            "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": res["cores"],
+                             "kind": "port", "sample": res["sample"]},
+            "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no", type=int, default=40)
     ap.add_argument("--nv", type=int, default=300)
     ap.add_argument("--seed", type=int, default=2)
-    ap.add_argument("--precision", default="DP")
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-terms", action="store_true")
     args = ap.parse_args()
     rank, world, local = dist_env()
-
     if args.impl == "reference":
-        res = cpu_reference(args, world, rank)
-        if res is None:
-            return
-        dt, tf, ncores, sample = res
-        line = {"metric": METRIC, "value": tf, "unit": "TFLOP/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "impl": "reference",
-                "config": {"workload": "RHF-CCSD iteration, synthetic Hamiltonian",
-                           "no": 20, "nv": 180, "seed": 1},
-                "cpu_baseline": {"value": tf, "unit": "TFLOP/s", "cores": ncores,
-                                 "kind": "port", "sample": sample},
-                "e2e": {"value": tf, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        reference_arm(args, rank)
         return
 
+    import numpy as np
     import torch
     import pycc_gb300 as pg
     from pycc_gb300 import _lib
+    if args.warmup < 3:
+        raise SystemExit("bench.py: at least 3 warm-up steps are required")
     dev = torch.device("cuda:%d" % local)
     torch.cuda.set_device(dev)
-    fac = pg.SyntheticFactors(args.no, args.nv, args.seed)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    o_n, v_n = args.no, args.nv
+    F_it = f_iter(o_n, v_n)
+    pk = peaks()
+
+    # ---- set-up: integral blocks built on the GPU from the 3-index factor ----------------
     t0 = time.time()
+    fac = pg.SyntheticFactors(o_n, v_n, args.seed, coupling="matched")
     H = pg.Hamiltonian.from_factors(fac, device=dev)
     torch.cuda.synchronize()
     setup_s = time.time() - t0
-    w = pg.CCwfn(H, precision=args.precision)
-    from pycc_gb300.diis import DIIS
-    diis = DIIS(w._amps, 8)
-    o, v = w.o, w.v
 
-    def step():
-        r1, r2 = w.residuals(H.F, w.t1, w.t2)
-        w.update_amplitudes(r1, r2)
-        w.cc_energy(o, v, H.F, H.L, w.t1, w.t2)
-        diis.add_error_vector(w._amps)
-        w._amps.copy_(diis.extrapolate(w._amps))
-
+    # ---- mixed-precision solve: W warm-up + K timed iterations ----------------------------
+    w = pg.CCwfn(H, precision="MIXED")
+    diis = w.start_iterations(8)
+    n = 0
     for _ in range(args.warmup):
-        step()
+        n += 1
+        w.iterate(diis, n)
+        w.diis_step(diis, n)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     clk = ClockSampler(local)
     clk.start()
+    l0 = _lib.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
     ev0.record()
     for _ in range(args.steps):
-        step()
+        n += 1
+        w.iterate(diis, n)
+        w.diis_step(diis, n)
     ev1.record()
     torch.cuda.synchronize()
+    launches = _lib.launch_count() - l0
     clocks = clk.stop()
     ms = ev0.elapsed_time(ev1) / args.steps
-    tf = f_iter(args.no, args.nv) / (ms * 1e-3) / 1e12
-    line = {"metric": METRIC, "value": tf, "unit": "TFLOP/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "DP" else "bf16", "data": "synthetic",
-            "config": {"workload": "RHF-CCSD iteration, synthetic Hamiltonian", "no": args.no,
-                       "nv": args.nv, "seed": args.seed, "precision": args.precision,
-                       "l2": "inputs larger than L2"},
-            "setup_s": setup_s, "clocks": clocks}
-    print(json.dumps(line))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    modes = w.mixed_engine().history[-args.steps:]
+    timed_energy = w.energies[-1]
+    # iterate on (untimed) to the precision floor for the converged mixed energy
+    e_mixed = None
+    for _ in range(60):
+        if w.mixed_engine().at_floor():
+            e_mixed = float(np.mean(w.energies[-4:]))
+            break
+        n += 1
+        w.iterate(diis, n)
+        w.diis_step(diis, n)
+
+    # ---- dominant kernel: per-GEMM CUDA events over one more iteration -------------------
+    eng = w.mixed_engine()
+    eng.tc.timing = []
+    n += 1
+    w.iterate(diis, n)
+    torch.cuda.synchronize()
+    recs = []
+    for r in eng.tc.timing:
+        recs.append({"subs": r["subs"], "fmt": r["fmt"], "M": r["M"], "N": r["N"], "Kp": r["Kp"],
+                     "ms": r["start"].elapsed_time(r["end"])})
+    eng.tc.timing = None
+    ladder = [r for r in recs if r["subs"] == "ijef,abef->ijab"]
+    roofline = None
+    if ladder:
+        lr = ladder[0]
+        alg = 2.0 * o_n**2 * v_n**4
+        npass = 3 if lr["fmt"] == 1 else 1
+        achieved = alg / (lr["ms"] * 1e-3) / 1e12
+        executed = npass * 2.0 * lr["M"] * lr["N"] * lr["Kp"] / (lr["ms"] * 1e-3) / 1e12
+        roofline = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16"],
+                    "unit": "TFLOP/s", "frac": achieved / pk["bf16"], "traffic": None,
+                    "kernel": "tc_gemm_kernel<256> ladder ijef,abef->ijab",
+                    "mode": {0: "bf16", 1: "bf16x3", 2: "fp8"}[lr["fmt"]],
+                    "executed_tflops": executed, "executed_frac": executed / pk["bf16"],
+                    "ms_per_launch": lr["ms"], "peak_source": pk["source"] + " bf16 burst"}
+    gemm_ms = sum(r["ms"] for r in recs)
+
+    # ---- e2e: public residuals() with host buffers ----------------------------------------
+    t1h = w.t1.detach().cpu().pin_memory()
+    t2h = w.t2.detach().cpu().pin_memory()
+    r1h = torch.empty_like(t1h).pin_memory()
+    r2h = torch.empty_like(t2h).pin_memory()
+    t1d = torch.empty_like(w.t1)
+    t2d = torch.empty_like(w.t2)
+
+    def e2e_step():
+        t1d.copy_(t1h, non_blocking=True)
+        t2d.copy_(t2h, non_blocking=True)
+        r1, r2 = w.residuals(H.F, t1d, t2d)
+        r1h.copy_(r1, non_blocking=True)
+        r2h.copy_(r2, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    e2e_step()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.e2e_steps):
+        e2e_step()
+    e1.record()
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+    nb = (t1h.numel() + t2h.numel()) * 8
+
+    # ---- plain FP64 form at the same size --------------------------------------------------
+    fp64 = None
+    if args.fp64_steps > 0:
+        w64 = pg.CCwfn(H, precision="DP")
+        d64 = w64.start_iterations(8)
+        small = pg.CCwfn(pg.Hamiltonian.from_factors(pg.SyntheticFactors(5, 19, 0), device=dev))
+        small.residuals(small.H.F, small.t1, small.t2)         # loads the FP64 kernels
+        torch.cuda.synchronize()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record()
+        for k in range(args.fp64_steps):
+            w64.iterate(d64, k + 1)
+            w64.diis_step(d64, k + 1)
+        f1.record()
+        torch.cuda.synchronize()
+        s64 = f0.elapsed_time(f1) / args.fp64_steps / 1e3
+        fp64 = {"s_per_iter": s64, "tflops": F_it / s64 / 1e12, "steps": args.fp64_steps,
+                "mixed_speedup": s64 / (ms * 1e-3)}
+        del w64, d64
+
+    # ---- FP64 oracle energy for the error of the mixed result ------------------------------
+    err = None
+    if os.path.exists(FP64_REF) and e_mixed is not None:
+        with open(FP64_REF) as f:
+            refs = json.load(f)
+        key = "%d_%d_%d" % (o_n, v_n, args.seed)
+        if key in refs:
+            err = abs(e_mixed - refs[key]["ecc"])
+
+    cpu = None
+    if not args.no_cpu_baseline and rank == 0:
+        res = cpu_oracle_iteration(1, 0)
+        cpu = {"value": res["tflops"], "unit": "TFLOP/s", "cores": res["cores"], "kind": "port",
+               "sample": res["sample"]}
+
+    line = {
+        "metric": METRIC, "value": F_it / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic",
+        "config": {"workload": "RHF-CCSD iteration (mixed precision ladder from the MP2 guess), "
+                               "synthetic Hamiltonian", "no": o_n, "nv": v_n, "seed": args.seed,
+                   "coupling": "matched (lambda=%.4f)" % fac.coupling,
+                   "l2": "inputs larger than L2 (integral blocks ~%.0f GB)" % (H.nbytes() / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "s_per_iter": ms * 1e-3, "modes_timed": modes, "energy_timed_last": timed_energy,
+        "energy_mixed": e_mixed, "energy_error_vs_fp64": err,
+        "fp64": fp64, "roofline": roofline, "cpu_baseline": cpu,
+        "e2e": {"value": F_it / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+                "what": "CCwfn.residuals with pinned-host t1/t2 in and r1/r2 out",
+                "ms_per_step": e2e_ms},
+        "gpu_launches": launches, "clocks": clocks, "setup_s": setup_s,
+        "gemm_ms_per_iter": gemm_ms,
+    }
+    if args.profile_terms:
+        line["terms"] = recs
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
 
 
 if __name__ == "__main__":

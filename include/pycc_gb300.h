@@ -19,6 +19,8 @@ extern "C" {
 /* ---- library ------------------------------------------------------------------------- */
 const char* pcg_last_error(void);
 int pcg_abi_version(void);
+/* number of kernels this library has launched since it was loaded */
+long long pcg_launch_count(void);
 /* compute capability of the current device as major*10+minor (103 on GB300) */
 int pcg_device_cc(void);
 int pcg_stream_sync(void* stream);
@@ -83,7 +85,7 @@ int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n
  *   rowoff_s(r) + koff_s(k); r (k) is a flat index over r_n (k_n) sub-indices with extents
  *   r_ext[q] and strides r_str[s*4 + q] for source s in (X, Y, P, Q) (0 = broadcast).
  *   fmt 0: BF16 into hi; 1: BF16 hi + BF16 lo = bf16(v - hi); 2: FP8 E4M3 into hi (bytes)
- *   with row_scale[r] = max_k |v| / 448.  Rows are Kp elements long (zero padded); Kp is a
+ *   with row_scale[r] = 2^ceil(log2(max_k |v| / 448)).  Rows are Kp elements long (zero padded); Kp is a
  *   multiple of 64 (BF16) or 128 (FP8).  Y, P, Q may be NULL. */
 int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* r_str, int k_n,
                      const long long* k_ext, const long long* k_str, long long Kp, double a,

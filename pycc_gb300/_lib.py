@@ -21,6 +21,7 @@ _d = C.c_double
 SIGNATURES = {
     "pcg_last_error": (C.c_char_p, []),
     "pcg_abi_version": (C.c_int, []),
+    "pcg_launch_count": (C.c_longlong, []),
     "pcg_device_cc": (C.c_int, []),
     "pcg_stream_sync": (C.c_int, [_p]),
     "pcg_contract_f64": (C.c_int, [C.c_int, _pi64, _pi64, _pi64, C.c_int, _pi64, _pi64, _pi64,
@@ -79,6 +80,11 @@ def call(name, *args):
         msg = lib.pcg_last_error().decode(errors="replace")
         raise EngineError("%s failed (%d): %s" % (name, rc, msg))
     return rc
+
+
+def launch_count() -> int:
+    """Kernels the CUDA library has launched since it was loaded."""
+    return int(load().pcg_launch_count())
 
 
 def stream_handle(stream=None):

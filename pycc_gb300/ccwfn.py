@@ -323,59 +323,94 @@ class CCwfn:
         return out
 
     # -- pycc/ccwfn.py:216-319 ------------------------------------------------------------
+    def start_iterations(self, max_diis=8):
+        """Energy of the current amplitudes and a fresh DIIS history (solve_cc set-up)."""
+        o, v, F, L = self.o, self.v, self.H.F, self.H.L
+        ecc = float(self.cc_energy(o, v, F, L, self.t1, self.t2))
+        self.energies = [ecc]
+        self.iter_times = []
+        self._last_rms = float('inf')
+        return DIIS(self._amps, max_diis, self.stream)
+
+    def iterate(self, diis, niter, start_diis=1, extrapolate=True):
+        """One Jacobi + DIIS iteration (ccwfn.py:270-319); returns (ecc, rms).
+
+        The precision schedule of the mixed engine is driven by the previous update norm.
+        DIIS bookkeeping runs when ``extrapolate`` is set (solve_cc skips it on the
+        iteration that converges, as the reference does).
+        """
+        t0 = time.time()
+        o, v, F, L = self.o, self.v, self.H.F, self.H.L
+        if self.precision in ('MIXED', 'SP'):
+            self.mixed_engine().select_mode(self._last_rms)
+        r1, r2 = self.residuals(F, self.t1, self.t2)
+        rms_t = self.update_amplitudes(r1, r2)
+        e_t = self.cc_energy(o, v, F, L, self.t1, self.t2)
+        del r1, r2
+        vals = torch.stack([e_t.reshape(()), rms_t.reshape(())]).cpu().numpy()
+        ecc, rms = float(vals[0]), math.sqrt(max(float(vals[1]), 0.0))
+        if self.precision in ('MIXED', 'SP'):
+            self.mixed_engine().tc.check_status()
+        self.energies.append(ecc)
+        self.iter_times.append(time.time() - t0)
+        self.niter = niter
+        self._last_rms = rms
+        if not (math.isfinite(ecc) and math.isfinite(rms)):
+            raise NumericalError("non-finite energy/update norm at iteration %d" % niter)
+        return ecc, rms
+
+    def diis_step(self, diis, niter, start_diis=1):
+        diis.add_error_vector(self._amps)
+        if niter >= start_diis:
+            self._amps.copy_(diis.extrapolate(self._amps))
+
     def solve_cc(self, e_conv=1e-7, r_conv=1e-7, maxiter=100, max_diis=8, start_diis=1,
                  callback=None):
         """Jacobi + DIIS iteration to convergence; returns the correlation energy (float).
 
+        Convergence: |dE| < e_conv and rms < r_conv (ccwfn.py:295).  In the MIXED / SP
+        modes the compensated products have a rounding floor; once the final precision
+        stage has stopped reducing the update norm for several iterations the energy is
+        reported as the mean of the last four iterates (``self.converged_at_floor``).
         Raises :class:`ConvergenceError` if ``maxiter`` is exhausted and
         :class:`NumericalError` if the energy or the update norm turns NaN/Inf.
         """
         t_start = time.time()
         self.e_conv, self.r_conv, self.maxiter = e_conv, r_conv, maxiter
-        o, v, F, L = self.o, self.v, self.H.F, self.H.L
-        ecc = float(self.cc_energy(o, v, F, L, self.t1, self.t2))
-        self.energies = [ecc]
-        self.iter_times = []
-        diis = DIIS(self._amps, max_diis, self.stream)
+        self.converged_at_floor = False
+        diis = self.start_iterations(max_diis)
+        ecc = self.energies[0]
         ediff, rms = -ecc, float('inf')
         for niter in range(1, maxiter + 1):
-            t0 = time.time()
             ecc_last = ecc
-            if self._mixed is not None or self.precision in ('MIXED', 'SP'):
-                self.mixed_engine().select_mode(rms)
-            r1, r2 = self.residuals(F, self.t1, self.t2)
-            rms_t = self.update_amplitudes(r1, r2)
-            e_t = self.cc_energy(o, v, F, L, self.t1, self.t2)
-            del r1, r2
-            vals = torch.stack([e_t.reshape(()), rms_t.reshape(())]).cpu().numpy()
-            ecc, rms = float(vals[0]), math.sqrt(max(float(vals[1]), 0.0))
+            ecc, rms = self.iterate(diis, niter, start_diis)
             ediff = ecc - ecc_last
-            self.energies.append(ecc)
-            self.iter_times.append(time.time() - t0)
-            self.niter = niter
-            if not (math.isfinite(ecc) and math.isfinite(rms)):
-                raise NumericalError("non-finite energy/update norm at iteration %d" % niter)
             if callback is not None:
                 callback(niter, ecc, ediff, rms)
             if not self.quiet:
                 print("%4d  %20.15f  %12.3e  %12.3e" % (niter, ecc, ediff, rms))
-            if abs(ediff) < e_conv and rms < r_conv:
-                if self.precision != 'DP' and not self.mixed_engine().is_final_mode():
-                    # converged in a low-precision mode: continue in the compensated mode
-                    self.mixed_engine().force_final()
-                else:
+            done = abs(ediff) < e_conv and rms < r_conv
+            if self.precision != 'DP':
+                eng = self.mixed_engine()
+                if done and not eng.is_final_mode():
+                    eng.force_final()          # converged in a fast stage: refine
+                    done = False
+                elif not done and eng.at_floor() and len(self.energies) > 4:
+                    ecc = float(np.mean(self.energies[-4:]))
+                    self.converged_at_floor = True
+                    self.rms_floor = rms
+                    done = True
+            if done:
+                self.ecc = ecc
+                self.timing["solve"] = time.time() - t_start
+                if self.model == 'CCSD(T)':
+                    from .triples import t_energy
+                    et = t_energy(self)
+                    self.et = et
+                    ecc = ecc + et
                     self.ecc = ecc
-                    self.timing["solve"] = time.time() - t_start
-                    if self.model == 'CCSD(T)':
-                        from .triples import t_energy
-                        et = t_energy(self)
-                        self.et = et
-                        ecc = ecc + et
-                        self.ecc = ecc
-                    return ecc
-            diis.add_error_vector(self._amps)
-            if niter >= start_diis:
-                self._amps.copy_(diis.extrapolate(self._amps))
+                return ecc
+            self.diis_step(diis, niter, start_diis)
         raise ConvergenceError("CCSD", maxiter, ediff, rms)
 
 

@@ -1,9 +1,13 @@
 // Library-wide C-ABI helpers: error text, version, device query.
 #include "common.cuh"
+#include <atomic>
 #include <cstring>
 
 namespace pcg {
 static thread_local char g_err[512] = {0};
+static std::atomic<long long> g_launches{0};
+
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const char* fmt, ...) {
   va_list ap;
@@ -16,6 +20,9 @@ void set_error(const char* fmt, ...) {
 extern "C" const char* pcg_last_error(void) { return pcg::g_err; }
 
 extern "C" int pcg_abi_version(void) { return 1; }
+
+// Kernels launched by this library since it was loaded (all threads, all streams).
+extern "C" long long pcg_launch_count(void) { return pcg::g_launches.load(); }
 
 // Compute capability of the current device as major*10+minor, or a negative CUDA error.
 extern "C" int pcg_device_cc(void) {

@@ -9,6 +9,8 @@ namespace pcg {
 
 // Host-side error text of the last failing entry point (per thread).
 void set_error(const char* fmt, ...);
+// Counts kernel launches issued by the library (read with pcg_launch_count).
+void note_launch();
 
 // Up to four sub-indices of one index group (M, N or K) of a contraction; each carries
 // its extent and its element stride in the two tensors that hold it.
@@ -52,6 +54,7 @@ enum DeviceStatus : int {
 
 #define PCG_CHECK_LAUNCH(name)                                                    \
   do {                                                                            \
+    pcg::note_launch();                                                           \
     cudaError_t _e = cudaGetLastError();                                          \
     if (_e != cudaSuccess) {                                                      \
       pcg::set_error("%s: launch failed: %s", name, cudaGetErrorString(_e));      \

@@ -254,6 +254,7 @@ extern "C" int pcg_update_amps_f64(double* t1, double* t2, const double* r1, con
   long long n = no * nv + no * no * nv * nv;
   int nb = std::min(ew_blocks(n), RED_BLOCKS);
   update_kernel<<<nb, EW_THREADS, 0, st>>>(t1, t2, r1, r2, eps, no, nv, work);
+  PCG_CHECK_LAUNCH("pcg_update_amps_f64/update");
   finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, 1, rms2);
   PCG_CHECK_LAUNCH("pcg_update_amps_f64");
   return 0;
@@ -270,6 +271,7 @@ extern "C" int pcg_energy_f64(const double* fov, const long long* fs, const doub
   long long n = no * nv + no * no * nv * nv;
   int nb = std::min(ew_blocks(n), RED_BLOCKS);
   energy_kernel<<<nb, EW_THREADS, 0, st>>>(fov, fs[0], fs[1], L, s, t1, t2, no, nv, work);
+  PCG_CHECK_LAUNCH("pcg_energy_f64/terms");
   finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, 1, out);
   PCG_CHECK_LAUNCH("pcg_energy_f64");
   return 0;
@@ -287,6 +289,7 @@ extern "C" int pcg_dots_f64(const double* x, const double* const* ys, int k, lon
   for (int j = 0; j < k; ++j) v.p[j] = ys[j];
   int nb = std::min(ew_blocks(n), RED_BLOCKS);
   dots_kernel<<<nb, EW_THREADS, 0, st>>>(x, v, k, n, work);
+  PCG_CHECK_LAUNCH("pcg_dots_f64/partials");
   finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, k, out);
   PCG_CHECK_LAUNCH("pcg_dots_f64");
   return 0;

@@ -400,9 +400,10 @@ __global__ void pack_fp8_kernel(const PackArgs p) {
   }
   __syncthreads();
   m = red[0];
-  const double s = (m > 0.0) ? m / 448.0 : 1.0;
+  // power-of-two scale: the smallest 2^e with max|v| / 2^e <= 448, so dequantisation is exact
+  const double s = (m > 0.0) ? exp2(ceil(log2(m / 448.0))) : 1.0;
   if (threadIdx.x == 0) p.scale[r] = (float)s;
-  const double inv = 1.0 / (double)(float)s;
+  const double inv = 1.0 / s;
   __nv_fp8_e4m3* dst = reinterpret_cast<__nv_fp8_e4m3*>(p.hi) + r * p.Kp;
   for (long long k = threadIdx.x; k < p.Kp; k += blockDim.x) {
     double v = (k < p.K) ? pack_value(p, ro, k) * inv : 0.0;

@@ -25,42 +25,87 @@ from .tc import FMT_BF16, FMT_BF16X3, FMT_FP8, Operand, TCEngine
 
 
 class MixedResidual:
+    """Precision ladder: FP8 ladder + BF16 -> BF16 -> split-BF16x3.
+
+    A stage hands over to the next when the update norm drops below its threshold or
+    stops decreasing (the stage's rounding floor): ``fp8_threshold`` (1e-3) for the FP8
+    stage, ``switch_threshold`` (1e-5) for BF16.
+    """
+
+    STALL_RATIO = 0.8     # rms above this fraction of the stage's best counts as no progress
+    STALL_ITERS = 2       # consecutive non-improving iterations that end a stage
+
     def __init__(self, w, mode="auto"):
         self.w = w
         self.tc = TCEngine(w.device1, w.stream)
-        self.fixed_final = mode == "bf16x3"
-        self.final = self.fixed_final
+        if mode == "bf16x3":
+            self.stages = ["bf16x3"]
+        else:
+            self.stages = (["fp8", "bf16", "bf16x3"] if w.vvvv_fp8 else ["bf16", "bf16x3"])
+        self.stage = 0
+        self.thresholds = {"fp8": getattr(w, "fp8_threshold", 1e-3), "bf16": w.switch_threshold}
+        self.best = float("inf")
+        self.bad = 0
         self.history = []
+        self.profile = None       # list of (subscripts, fmt, start, end) events when set
 
     # -- precision schedule ---------------------------------------------------------------
     def select_mode(self, rms):
-        if not self.fixed_final and rms < self.w.switch_threshold:
-            self.final = True
+        """Pick the precision of the next residual from the last update norm."""
+        if rms < float("inf"):
+            name = self.stages[self.stage]
+            if not self.is_final_mode() and rms < self.thresholds.get(name, 0.0):
+                self._advance()
+            else:
+                if rms > self.STALL_RATIO * self.best:
+                    self.bad += 1
+                else:
+                    self.bad = 0
+                self.best = min(self.best, rms)
+                if self.bad >= self.STALL_ITERS and not self.is_final_mode():
+                    self._advance()
+        if rms == 0.0:                      # explicit request for the final stage
+            self.stage = len(self.stages) - 1
         self.history.append(self.mode_name())
 
+    def _advance(self):
+        self.stage = min(self.stage + 1, len(self.stages) - 1)
+        self.best = float("inf")
+        self.bad = 0
+
+    def at_floor(self):
+        """True once the final stage has stopped reducing the update norm."""
+        return self.is_final_mode() and self.bad >= 2 * self.STALL_ITERS
+
     def force_final(self):
-        self.final = True
+        self.stage = len(self.stages) - 1
 
     def is_final_mode(self):
-        return self.final
+        return self.stage == len(self.stages) - 1
 
     def mode_name(self):
-        if self.final:
-            return "bf16x3"
-        return "bf16+fp8" if self.w.vvvv_fp8 else "bf16"
+        return self.stages[self.stage]
 
     def fmt(self):
-        return FMT_BF16X3 if self.final else FMT_BF16
+        return FMT_BF16X3 if self.mode_name() == "bf16x3" else FMT_BF16
 
     def ladder_fmt(self):
-        if self.final:
-            return FMT_BF16X3
-        return FMT_FP8 if self.w.vvvv_fp8 else FMT_BF16
+        name = self.mode_name()
+        return {"fp8": FMT_FP8, "bf16": FMT_BF16, "bf16x3": FMT_BF16X3}[name]
 
     # -- helpers --------------------------------------------------------------------------
     def tcc(self, subs, A, B, out, alpha=1.0, beta=1.0, fmt=None):
-        return self.tc.contract(subs, A, B, out, alpha=alpha, beta=beta,
-                                fmt=self.fmt() if fmt is None else fmt)
+        fmt = self.fmt() if fmt is None else fmt
+        if self.profile is None:
+            return self.tc.contract(subs, A, B, out, alpha=alpha, beta=beta, fmt=fmt)
+        # per-term timing: CUDA events on the launching stream around pack + GEMM
+        st = torch.cuda.current_stream() if self.w.stream is None else self.w.stream
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        res = self.tc.contract(subs, A, B, out, alpha=alpha, beta=beta, fmt=fmt)
+        e1.record(st)
+        self.profile.append((subs, fmt, e0, e1))
+        return res
 
     def eri(self, pat, labels):
         return Operand.of(labels, self.w.H.ERI.blocks[pat], key=("ERI", pat))

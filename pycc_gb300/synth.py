@@ -18,6 +18,15 @@ Draw order (fixed so that every consumer sees the same arrays)::
     (pq|rs) = sum_Q B[Q,p,q] B[Q,r,s]
 
 The chemist tensor is positive semi-definite with full 8-fold permutational symmetry.
+
+Coupling scale.  With the plain sigma above, the pair-coupling strength
+``o^2 v^2 var(<ij|ab>) ~ o^2 v^2 (0.35^2)^2 / naux`` grows with the size: at no=5, nv=19 the
+CCSD energy is -0.73 Eh and the iteration converges, but at no=20, nv=180 the MP2 energy
+is already about -160 Eh and the CCSD iteration diverges (for the reference and for this
+engine alike).  ``coupling`` multiplies sigma by lambda; ``coupling='matched'`` picks
+lambda = (125.35 naux / (o^2 v^2))^(1/4), which keeps o^2 v^2 var(<ij|ab>) at its
+no=5, nv=19 value (lambda = 1 there exactly) so every size is a convergent, moderately
+correlated problem.  The draw order and every other distribution are unchanged.
 The full ``nmo^4`` tensors are only built on the host for small sizes; large problems
 build the needed ``o/v`` blocks on the GPU from ``B`` (see ``pycc_gb300.hamiltonian``).
 """
@@ -38,18 +47,21 @@ CONFIGS = {
 class SyntheticFactors:
     """Orbital energies and the symmetric 3-index factor ``B[Q,p,q]`` of one Hamiltonian."""
 
-    def __init__(self, no: int, nv: int, seed: int, naux: int | None = None):
+    def __init__(self, no: int, nv: int, seed: int, naux: int | None = None, coupling=1.0):
         self.no = int(no)
         self.nv = int(nv)
         self.nmo = self.no + self.nv
         self.naux = int(naux) if naux is not None else 3 * self.nmo
         self.seed = int(seed)
+        if coupling == "matched":
+            coupling = matched_coupling(self.no, self.nv, self.naux)
+        self.coupling = float(coupling)
         n = self.nmo
         rng = np.random.default_rng(self.seed)
         eps_o = np.sort(rng.uniform(-1.2, -0.4, self.no))
         eps_v = np.sort(rng.uniform(0.3, 2.5, self.nv))
         self.eps = np.concatenate((eps_o, eps_v))
-        sigma = 0.35 / np.sqrt(self.naux)
+        sigma = self.coupling * 0.35 / np.sqrt(self.naux)
         iu = np.triu_indices(n)
         draws = rng.normal(0.0, sigma, size=(self.naux, iu[0].size))
         B = np.empty((self.naux, n, n))
@@ -84,6 +96,17 @@ class SyntheticFactors:
         return self.F, ERI, L
 
 
-def synthetic_factors(config: int) -> SyntheticFactors:
+#: o^2 v^2 / naux at no=5, nv=19 (naux=72): the coupling strength 'matched' keeps.
+_REF_STRENGTH = (5 * 5 * 19 * 19) / 72.0
+
+
+def matched_coupling(no: int, nv: int, naux: int) -> float:
+    """lambda with lambda^4 o^2 v^2 / naux equal to its no=5, nv=19 value."""
+    if (no, nv, naux) == (5, 19, 72):
+        return 1.0
+    return float((_REF_STRENGTH * naux / float(no * no * nv * nv)) ** 0.25)
+
+
+def synthetic_factors(config: int, coupling=1.0) -> SyntheticFactors:
     no, nv, seed = CONFIGS[config]
-    return SyntheticFactors(no, nv, seed)
+    return SyntheticFactors(no, nv, seed, coupling=coupling)

@@ -171,6 +171,7 @@ class TCEngine:
         self.stream = stream
         self.status = torch.zeros(4, dtype=torch.int32, device=device)
         self.cache = {}
+        self.timing = None        # list of GEMM launch records (CUDA events) when set
 
     def cached_bytes(self):
         return sum(p.nbytes() for p in self.cache.values())
@@ -200,14 +201,24 @@ class TCEngine:
             A, B, ma, nb = B, A, nb, ma
         pa = self._pack(A, ma, kk, fmt, "A")
         pb = self._pack(B, nb, kk, fmt, "B")
+        ev = None
+        if self.timing is not None:
+            st = torch.cuda.current_stream() if self.stream is None else self.stream
+            ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+            ev[0].record(st)
         gemm(fmt, pa, pb, out, ma, nb, rhs, alpha=alpha, beta=beta, status=self.status,
              stream=self.stream)
+        if ev is not None:
+            ev[1].record(st)
+            self.timing.append({"subs": subscripts, "fmt": fmt, "M": pa.rows, "N": pb.rows,
+                                "Kp": pa.Kp, "start": ev[0], "end": ev[1]})
         return out
 
     def _pack(self, op, rows, ks, fmt, side):
         if op.key is None:
             return pack(op, rows, ks, fmt, self.stream)
-        key = (op.key, tuple(rows), tuple(ks), fmt)
+        # the operand's own label string fixes which tensor axis each label names
+        key = (op.key, op.labels, tuple(rows), tuple(ks), fmt)
         p = self.cache.get(key)
         if p is None:
             p = pack(op, rows, ks, fmt, self.stream)

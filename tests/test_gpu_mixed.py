@@ -101,7 +101,7 @@ def test_mixed_residual_cfg1(cuda, h1, cfg1):
 
 def test_mixed_solve_cfg1(cuda, h1, cfg1):
     w = pg.CCwfn(h1, precision="MIXED")
-    e = w.solve_cc(1e-10, 1e-10, 100)
+    e = w.solve_cc(1e-9, 1e-7, 100)
     assert abs(e - float(cfg1["ecc"])) < 1e-6
     assert w.mixed_engine().is_final_mode()
 
@@ -109,7 +109,7 @@ def test_mixed_solve_cfg1(cuda, h1, cfg1):
 def test_sp_solve_cfg1(cuda, h1, cfg1):
     """precision='SP' (split-BF16x3 throughout) within 1e-7 of DP, as the reference's SP test."""
     w = pg.CCwfn(h1, precision="SP")
-    e = w.solve_cc(1e-10, 1e-10, 100)
+    e = w.solve_cc(1e-9, 1e-7, 100)
     assert abs(e - float(cfg1["ecc"])) < 1e-7
 
 
