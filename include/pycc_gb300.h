@@ -78,31 +78,37 @@ int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n
                     void* stream);
 
 /* ---- tensor-core (tcgen05) contraction engine, mixed-precision path ------------------
- * The GB300 replacement of the BF16/FP8 path of the same contractions (pycc/ccwfn.py:
- * 458-945 through pycc/device.py:64-87); the reference has no low-precision path of its own.
+ * The GB300 replacement of the low-precision path of the same contractions (pycc/ccwfn.py:
+ * 458-945 through pycc/device.py:64-87); the reference's own low-precision mode is plain
+ * float32 (pycc/device.py:143-154).
  *
  * pcg_pack_operand: dst[r][k] = convert(a*X + b*Y + c*P*Q), each source read at
  *   rowoff_s(r) + koff_s(k); r (k) is a flat index over r_n (k_n) sub-indices with extents
  *   r_ext[q] and strides r_str[s*4 + q] for source s in (X, Y, P, Q) (0 = broadcast).
- *   fmt 0: BF16 into hi; 1: BF16 hi + BF16 lo = bf16(v - hi); 2: FP8 E4M3 into hi (bytes)
- *   with row_scale[r] = 2^ceil(log2(max_k |v| / 448)).  Rows are Kp elements long (zero padded); Kp is a
- *   multiple of 64 (BF16) or 128 (FP8).  Y, P, Q may be NULL. */
+ *   Formats: 0 BF16 into hi; 1 BF16 hi + lo = bf16(v - hi); 2 FP8 E4M3 bytes into hi with
+ *   row_scale[r] = 2^ceil(log2(max_k |v| / 448)); 3 three BF16 pieces hi = bf16(v),
+ *   mid = bf16(v - hi), lo = bf16(v - hi - mid).  Rows are Kp elements long (zero padded);
+ *   Kp is a multiple of 64 (BF16) or 128 (FP8).  X or P (with Q) must be given; Y may be
+ *   NULL; mid is used by format 3 only. */
 int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* r_str, int k_n,
                      const long long* k_ext, const long long* k_str, long long Kp, double a,
                      const double* X, double b, const double* Y, double c, const double* P,
-                     const double* Q, void* hi, void* lo, float* row_scale, void* stream);
+                     const double* Q, void* hi, void* mid, void* lo, float* row_scale,
+                     void* stream);
 
 /* pcg_tc_gemm: C[off_m(m) + off_n(n)] = beta*C + alpha * sum_k A[m][k] B[n][k] (C FP64).
  *   A: M rows of lda elements (K-major, 16-byte aligned rows), B: N rows of ldb elements;
- *   fmt as above (1 = three tcgen05 passes Ah.Bh + Ah.Bl + Al.Bh; 2 = FP8 with the row
- *   scales applied in the epilogue).  off_m / off_n: flat index over up to 4 sub-indices
- *   (extents, element strides in C).  status: device int, set non-zero when a bounded
- *   device-side wait expired (the kernel then skips its stores). */
-int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_lo, long long M, long long lda,
-                const void* B_hi, const void* B_lo, long long N, long long ldb, long long Kp,
-                const float* a_scale, const float* b_scale, int m_n, const long long* m_ext,
-                const long long* m_sc, int n_n, const long long* n_ext, const long long* n_sc,
-                double alpha, double beta, double* C, int* status, void* stream);
+ *   format as above: 1 = three tcgen05 passes Al.Bh + Ah.Bl + Ah.Bh, 3 = the six piece
+ *   products of order <= 2^-16 (smallest first), 2 = FP8 with the row scales applied in the
+ *   epilogue.  off_m / off_n: flat index over up to 4 sub-indices (extents, element strides
+ *   in C).  status: device int, set non-zero when a bounded device-side wait expired (the
+ *   kernel then skips its stores). */
+int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, long long M,
+                long long lda, const void* B_hi, const void* B_mid, const void* B_lo, long long N,
+                long long ldb, long long Kp, const float* a_scale, const float* b_scale, int m_n,
+                const long long* m_ext, const long long* m_sc, int n_n, const long long* n_ext,
+                const long long* n_sc, double alpha, double beta, double* C, int* status,
+                void* stream);
 
 #ifdef __cplusplus
 }

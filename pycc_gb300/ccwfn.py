@@ -12,8 +12,8 @@ the same method names, argument orders and return layouts -- ``build_tau``,
   (``pycc_gb300.mixed``): BF16 operands with FP32 accumulation (FP8 with per-row scales for
   the <ab|ef> ladder), switching to compensated split-BF16x3 products once the update norm
   drops below ``switch_threshold``; amplitudes, denominators, energy, norms and DIIS stay FP64.
-* ``precision='SP'``: every contraction in split-BF16x3 (single-precision class accuracy),
-  FP64 amplitudes.
+* ``precision='SP'``: every contraction in three-piece split-BF16 (six tcgen05 products,
+  FP32-class accuracy, the analogue of the reference's float32 mode); FP64 amplitudes.
 
 There is no CPU fallback: ``device='CPU'`` is the reference's own code path.
 """
@@ -297,7 +297,7 @@ class CCwfn:
     def mixed_engine(self):
         if self._mixed is None:
             from .mixed import MixedResidual
-            self._mixed = MixedResidual(self, mode='bf16x3' if self.precision == 'SP' else 'auto')
+            self._mixed = MixedResidual(self, mode='bf16x6' if self.precision == 'SP' else 'auto')
         return self._mixed
 
     # -- pycc/ccwfn.py:1122-1162 ----------------------------------------------------------

@@ -30,7 +30,22 @@ constexpr int KBYTES = 128;            // bytes of K per stage row (one 128B swi
 constexpr int NT = 128;
 constexpr unsigned long long kWaitNs = 4000000000ull;  // 4 s bound on any single wait
 
-enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2 };
+enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2, kBF16x6 = 3 };
+
+// Operand pieces multiplied in each pass (A piece, B piece), smallest products first so
+// the FP32 accumulator sums the small corrections before the leading term.
+//   BF16x3: v = hi + lo;        Ah.Bh + Ah.Bl + Al.Bh
+//   BF16x6: v = hi + mid + lo;  the six products of order <= 2^-16
+constexpr int kMaxPass = 6;
+struct PassTable {
+  int n;
+  unsigned char a[kMaxPass], b[kMaxPass];
+};
+
+struct Maps {
+  CUtensorMap a[3];
+  CUtensorMap b[3];
+};
 
 struct EpiIdx {
   int n;
@@ -43,7 +58,8 @@ struct Args {
   int nkb;          // K blocks per pass in this split
   int kb_per_split; // K blocks handled by one split (blockIdx.z)
   int nkb_total;    // K blocks of the whole K range
-  int npass;        // 1, or 3 for split-BF16x3
+  int npass;        // 1, 3 (split-BF16x3) or 6 (split-BF16x6)
+  PassTable pt;
   int fp8;
   EpiIdx em, en;
   double alpha, beta;
@@ -169,9 +185,7 @@ struct Smem {
 
 template <int BN>
 __global__ void __launch_bounds__(NT, 1)
-    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmAh, const __grid_constant__ CUtensorMap tmAl,
-                   const __grid_constant__ CUtensorMap tmBh, const __grid_constant__ CUtensorMap tmBl,
-                   const Args p) {
+    tc_gemm_kernel(const __grid_constant__ Maps maps, const Args p) {
   using L = Smem<BN>;
   constexpr int S = L::STAGES;
   extern __shared__ uint8_t smem_raw[];
@@ -234,8 +248,8 @@ __global__ void __launch_bounds__(NT, 1)
         if (*abort_flag) break;
         const int pass = it / nkb;
         const int kb = kb0 + (it % nkb);
-        const CUtensorMap* ta = (pass == 2) ? &tmAl : &tmAh;
-        const CUtensorMap* tb = (pass == 1) ? &tmBl : &tmBh;
+        const CUtensorMap* ta = &maps.a[p.pt.a[pass]];
+        const CUtensorMap* tb = &maps.b[p.pt.b[pass]];
         const int kx = kb * (p.fp8 ? 128 : 64);
         mbar_expect_tx(&full[s], bytes);
         tma_load_2d(ta, &full[s], sA + s * L::A_BYTES, kx, (int)m0);
@@ -351,6 +365,7 @@ struct PackArgs {
   const double* Q;
   void* hi;
   void* lo;
+  void* mid;
   float* scale;
   int fmt;
 };
@@ -373,11 +388,18 @@ __global__ void pack_bf16_kernel(const PackArgs p) {
   pack_offsets(p.r, r, ro);
   __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(p.hi) + r * p.Kp;
   __nv_bfloat16* lo = p.lo ? reinterpret_cast<__nv_bfloat16*>(p.lo) + r * p.Kp : nullptr;
+  __nv_bfloat16* mid = p.mid ? reinterpret_cast<__nv_bfloat16*>(p.mid) + r * p.Kp : nullptr;
   for (long long k = threadIdx.x; k < p.Kp; k += blockDim.x) {
     double v = (k < p.K) ? pack_value(p, ro, k) : 0.0;
     __nv_bfloat16 h = __double2bfloat16(v);
     hi[k] = h;
-    if (lo) lo[k] = __double2bfloat16(v - (double)__bfloat162float(h));
+    double rest = v - (double)__bfloat162float(h);
+    if (mid) {
+      __nv_bfloat16 m = __double2bfloat16(rest);
+      mid[k] = m;
+      rest -= (double)__bfloat162float(m);
+    }
+    if (lo) lo[k] = __double2bfloat16(rest);
   }
 }
 
@@ -474,8 +496,7 @@ int num_sms() {
 }
 
 template <int BN>
-int launch(const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh,
-           const CUtensorMap& bl, const Args& a, long long mt, long long nt, int splits,
+int launch(const Maps& maps, const Args& a, long long mt, long long nt, int splits,
            cudaStream_t st) {
   static bool attr = false;
   const int smem = Smem<BN>::TOTAL;
@@ -484,7 +505,7 @@ int launch(const CUtensorMap& ah, const CUtensorMap& al, const CUtensorMap& bh,
     attr = true;
   }
   dim3 grid((unsigned)nt, (unsigned)mt, (unsigned)splits);
-  tc_gemm_kernel<BN><<<grid, NT, smem, st>>>(ah, al, bh, bl, a);
+  tc_gemm_kernel<BN><<<grid, NT, smem, st>>>(maps, a);
   PCG_CHECK_LAUNCH("pcg_tc_gemm");
   return 0;
 }
@@ -541,11 +562,11 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
                                 int k_n, const long long* k_ext, const long long* k_str,
                                 long long Kp, double a, const double* X, double b,
                                 const double* Y, double c, const double* P, const double* Q,
-                                void* hi, void* lo, float* row_scale, void* stream) {
+                                void* hi, void* mid, void* lo, float* row_scale, void* stream) {
   PackArgs p{};
   if (!fill_pack(p.r, r_n, r_ext, r_str) || !fill_pack(p.k, k_n, k_ext, k_str)) return -1;
-  if ((!X && !P) || !hi || (fmt == kBF16x3 && !lo) || (fmt == kFP8 && !row_scale) || (P && !Q) ||
-      fmt < 0 || fmt > 2) {
+  if (fmt < 0 || fmt > 3 || (!X && !P) || !hi || ((fmt == kBF16x3 || fmt == kBF16x6) && !lo) ||
+      (fmt == kBF16x6 && !mid) || (fmt == kFP8 && !row_scale) || (P && !Q)) {
     set_error("pcg_pack_operand: bad pointers for format %d", fmt);
     return -1;
   }
@@ -567,7 +588,8 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   p.P = P;
   p.Q = Q;
   p.hi = hi;
-  p.lo = (fmt == kBF16x3) ? lo : nullptr;
+  p.lo = (fmt == kBF16x3 || fmt == kBF16x6) ? lo : nullptr;
+  p.mid = (fmt == kBF16x6) ? mid : nullptr;
   p.scale = row_scale;
   p.fmt = fmt;
   dim3 grid((unsigned)std::min<long long>(p.R, 65535), (unsigned)((p.R + 65534) / 65535));
@@ -580,21 +602,22 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   return 0;
 }
 
-extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_lo, long long M,
-                           long long lda, const void* B_hi, const void* B_lo, long long N,
-                           long long ldb, long long Kp, const float* a_scale,
-                           const float* b_scale, int m_n, const long long* m_ext,
-                           const long long* m_sc, int n_n, const long long* n_ext,
-                           const long long* n_sc, double alpha, double beta, double* C,
-                           int* status, void* stream) {
-  if (fmt < 0 || fmt > 2) {
+extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo,
+                           long long M, long long lda, const void* B_hi, const void* B_mid,
+                           const void* B_lo, long long N, long long ldb, long long Kp,
+                           const float* a_scale, const float* b_scale, int m_n,
+                           const long long* m_ext, const long long* m_sc, int n_n,
+                           const long long* n_ext, const long long* n_sc, double alpha,
+                           double beta, double* C, int* status, void* stream) {
+  if (fmt < 0 || fmt > 3) {
     set_error("pcg_tc_gemm: unknown format %d", fmt);
     return -1;
   }
   const int eb = (fmt == kFP8) ? 1 : 2;
   const int kblk = KBYTES / eb;
-  if (!A_hi || !B_hi || !C || !status || (fmt == kBF16x3 && (!A_lo || !B_lo)) ||
-      (fmt == kFP8 && (!a_scale || !b_scale))) {
+  const bool need_lo = (fmt == kBF16x3 || fmt == kBF16x6);
+  if (!A_hi || !B_hi || !C || !status || (need_lo && (!A_lo || !B_lo)) ||
+      (fmt == kBF16x6 && (!A_mid || !B_mid)) || (fmt == kFP8 && (!a_scale || !b_scale))) {
     set_error("pcg_tc_gemm: null pointer for format %d", fmt);
     return -1;
   }
@@ -603,7 +626,7 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_lo, long lon
     set_error("pcg_tc_gemm: bad sizes M=%lld N=%lld Kp=%lld lda=%lld ldb=%lld", M, N, Kp, lda, ldb);
     return -1;
   }
-  const void* ptrs[4] = {A_hi, A_lo, B_hi, B_lo};
+  const void* ptrs[6] = {A_hi, A_mid, A_lo, B_hi, B_mid, B_lo};
   for (const void* q : ptrs)
     if (q && ((uintptr_t)q % 16) != 0) {
       set_error("pcg_tc_gemm: operand base not 16-byte aligned");
@@ -617,7 +640,12 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_lo, long lon
   a.M = M;
   a.N = N;
   a.fp8 = (fmt == kFP8);
-  a.npass = (fmt == kBF16x3) ? 3 : 1;
+  // pieces: 0 = hi, 1 = mid (BF16x6) or lo (BF16x3), 2 = lo (BF16x6)
+  static const PassTable t1 = {1, {0}, {0}};
+  static const PassTable t3 = {3, {1, 0, 0}, {0, 1, 0}};
+  static const PassTable t6 = {6, {2, 1, 0, 1, 0, 0}, {0, 1, 2, 0, 1, 0}};
+  a.pt = (fmt == kBF16x3) ? t3 : (fmt == kBF16x6 ? t6 : t1);
+  a.npass = a.pt.n;
   if (!fill_epi(a.em, m_n, m_ext, m_sc, "M") || !fill_epi(a.en, n_n, n_ext, n_sc, "N")) return -1;
   a.alpha = alpha;
   a.beta = beta;
@@ -650,14 +678,16 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_lo, long lon
     scale_epi_kernel<<<blocks, 256, 0, st>>>(a.em, a.en, M, N, beta, C);
     PCG_CHECK_LAUNCH("pcg_tc_gemm/scale");
   }
-  CUtensorMap ah, al, bh, bl;
-  if (!make_map(&ah, A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
-  if (!make_map(&al, A_lo ? A_lo : A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
-  if (!make_map(&bh, B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
-  if (!make_map(&bl, B_lo ? B_lo : B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
+  Maps maps;
+  const void* pa[3] = {A_hi, fmt == kBF16x6 ? A_mid : A_lo, A_lo};
+  const void* pb[3] = {B_hi, fmt == kBF16x6 ? B_mid : B_lo, B_lo};
+  for (int q = 0; q < 3; ++q) {
+    if (!make_map(&maps.a[q], pa[q] ? pa[q] : A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
+    if (!make_map(&maps.b[q], pb[q] ? pb[q] : B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
+  }
   switch (BN) {
-    case 64: return launch<64>(ah, al, bh, bl, a, mt, nt, splits, st);
-    case 128: return launch<128>(ah, al, bh, bl, a, mt, nt, splits, st);
-    default: return launch<256>(ah, al, bh, bl, a, mt, nt, splits, st);
+    case 64: return launch<64>(maps, a, mt, nt, splits, st);
+    case 128: return launch<128>(maps, a, mt, nt, splits, st);
+    default: return launch<256>(maps, a, mt, nt, splits, st);
   }
 }

@@ -21,7 +21,7 @@ import torch
 
 from . import _lib
 from .contract import contract_f64
-from .tc import FMT_BF16, FMT_BF16X3, FMT_FP8, Operand, TCEngine
+from .tc import FMT_BF16, FMT_BF16X3, FMT_BF16X6, FMT_FP8, Operand, TCEngine
 
 
 class MixedResidual:
@@ -38,7 +38,9 @@ class MixedResidual:
     def __init__(self, w, mode="auto"):
         self.w = w
         self.tc = TCEngine(w.device1, w.stream)
-        if mode == "bf16x3":
+        if mode == "bf16x6":
+            self.stages = ["bf16x6"]
+        elif mode == "bf16x3":
             self.stages = ["bf16x3"]
         else:
             self.stages = (["fp8", "bf16", "bf16x3"] if w.vvvv_fp8 else ["bf16", "bf16x3"])
@@ -86,12 +88,14 @@ class MixedResidual:
     def mode_name(self):
         return self.stages[self.stage]
 
+    FMTS = {"bf16": FMT_BF16, "bf16x3": FMT_BF16X3, "bf16x6": FMT_BF16X6, "fp8": FMT_BF16}
+
     def fmt(self):
-        return FMT_BF16X3 if self.mode_name() == "bf16x3" else FMT_BF16
+        return self.FMTS[self.mode_name()]
 
     def ladder_fmt(self):
         name = self.mode_name()
-        return {"fp8": FMT_FP8, "bf16": FMT_BF16, "bf16x3": FMT_BF16X3}[name]
+        return FMT_FP8 if name == "fp8" else self.FMTS[name]
 
     # -- helpers --------------------------------------------------------------------------
     def tcc(self, subs, A, B, out, alpha=1.0, beta=1.0, fmt=None):

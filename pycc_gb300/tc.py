@@ -20,7 +20,7 @@ import torch
 
 from . import _lib
 
-FMT_BF16, FMT_BF16X3, FMT_FP8 = 0, 1, 2
+FMT_BF16, FMT_BF16X3, FMT_FP8, FMT_BF16X6 = 0, 1, 2, 3
 MAX_SUB = 4
 
 
@@ -90,12 +90,13 @@ def _ptr(s):
 class Packed:
     """A packed K-major operand: ``hi`` (and ``lo`` / ``scale``) of shape [rows, Kp]."""
 
-    def __init__(self, fmt, rows, Kp, hi, lo=None, scale=None):
+    def __init__(self, fmt, rows, Kp, hi, lo=None, scale=None, mid=None):
         self.fmt, self.rows, self.Kp = fmt, rows, Kp
-        self.hi, self.lo, self.scale = hi, lo, scale
+        self.hi, self.lo, self.scale, self.mid = hi, lo, scale, mid
 
     def nbytes(self):
-        return sum(t.numel() * t.element_size() for t in (self.hi, self.lo, self.scale) if t is not None)
+        return sum(t.numel() * t.element_size() for t in (self.hi, self.mid, self.lo, self.scale)
+                   if t is not None)
 
 
 def kblock(fmt):
@@ -114,13 +115,15 @@ def pack(op: Operand, row_labels, k_labels, fmt, stream=None) -> Packed:
     kb = kblock(fmt)
     Kp = ((K + kb - 1) // kb) * kb
     dev = op.device()
+    mid = None
     if fmt == FMT_FP8:
         hi = torch.empty((R, Kp), dtype=torch.uint8, device=dev)
         lo = None
         scale = torch.empty(R, dtype=torch.float32, device=dev)
     else:
         hi = torch.empty((R, Kp), dtype=torch.bfloat16, device=dev)
-        lo = torch.empty_like(hi) if fmt == FMT_BF16X3 else None
+        lo = torch.empty_like(hi) if fmt in (FMT_BF16X3, FMT_BF16X6) else None
+        mid = torch.empty_like(hi) if fmt == FMT_BF16X6 else None
         scale = None
 
     def flat(groups):
@@ -135,9 +138,10 @@ def pack(op: Operand, row_labels, k_labels, fmt, stream=None) -> Packed:
     kn, ke, kst = flat(ks)
     _lib.call("pcg_pack_operand", int(fmt), rn, re_, rs, kn, ke, kst, Kp,
               float(op.a), _ptr(op.X), float(op.b), _ptr(op.Y), float(op.c), _ptr(op.P),
-              _ptr(op.Q), hi.data_ptr(), lo.data_ptr() if lo is not None else None,
+              _ptr(op.Q), hi.data_ptr(), mid.data_ptr() if mid is not None else None,
+              lo.data_ptr() if lo is not None else None,
               scale.data_ptr() if scale is not None else None, _lib.stream_handle(stream))
-    return Packed(fmt, R, Kp, hi, lo, scale)
+    return Packed(fmt, R, Kp, hi, lo, scale, mid)
 
 
 def gemm(fmt, A: Packed, B: Packed, out, row_labels, col_labels, out_labels, alpha=1.0,
@@ -152,9 +156,10 @@ def gemm(fmt, A: Packed, B: Packed, out, row_labels, col_labels, out_labels, alp
     if len(mg) > MAX_SUB or len(ng) > MAX_SUB:
         raise ValueError("gemm: more than %d output sub-indices" % MAX_SUB)
     i64 = _lib.i64s
-    _lib.call("pcg_tc_gemm", int(fmt), A.hi.data_ptr(), A.lo.data_ptr() if A.lo is not None else None,
-              A.rows, A.Kp, B.hi.data_ptr(), B.lo.data_ptr() if B.lo is not None else None,
-              B.rows, B.Kp, A.Kp,
+    def p(t):
+        return t.data_ptr() if t is not None else None
+    _lib.call("pcg_tc_gemm", int(fmt), p(A.hi), p(A.mid), p(A.lo), A.rows, A.Kp,
+              p(B.hi), p(B.mid), p(B.lo), B.rows, B.Kp, A.Kp,
               A.scale.data_ptr() if A.scale is not None else None,
               B.scale.data_ptr() if B.scale is not None else None,
               len(mg), i64([g[0] for g in mg]), i64([g[1][0] for g in mg]),

@@ -114,3 +114,47 @@ def test_ragged_sizes_vs_oracle(cuda, no, nv):
     w = pg.CCwfn(pg.Hamiltonian.from_factors(fac, device=cuda))
     r1, r2 = w.residuals(w.H.F, dev(t1, cuda), dev(t2, cuda))
     assert rel(r1, r1o) < 1e-11 and rel(r2, r2o) < 1e-11
+
+
+def _probe(no, nv, t2_mp2, seed):
+    rng = np.random.default_rng(1000 + seed)
+    t1 = 0.02 * rng.standard_normal((no, nv))
+    noise = 0.01 * rng.standard_normal((no, no, nv, nv))
+    return t1, t2_mp2 + noise + noise.transpose(1, 0, 3, 2)
+
+
+@pytest.fixture(scope="module")
+def cfg2_data():
+    from conftest import golden
+    return golden("cfg2.npz"), golden("cfg2_raw.npz")
+
+
+@pytest.mark.parametrize("which", ["matched", "raw"])
+def test_residual_cfg2_vs_reference(cuda, cfg2_data, which):
+    """no=20, nv=180: GPU FP64 residual against the reference's own output (both couplings)."""
+    g = cfg2_data[0] if which == "matched" else cfg2_data[1]
+    fac = pg.SyntheticFactors(20, 180, 1, coupling="matched" if which == "matched" else 1.0)
+    H = pg.Hamiltonian.from_factors(fac, device=cuda)
+    w = pg.CCwfn(H)
+    t1, t2 = _probe(20, 180, w.t2.cpu().numpy(), 1)
+    r1, r2 = w.residuals(H.F, dev(t1, cuda), dev(t2, cuda))
+    r2 = r2.cpu().numpy()
+    assert rel(r1, g["r1"]) < RTOL
+    assert rel(r2[0, 1], g["r2_slice_ij01"]) < RTOL
+    assert rel(r2[:, :, 0, 0], g["r2_slice_ab00"]) < RTOL
+    assert rel(r2[3, 3, 10:20, 100:110], g["r2_slice_diag"]) < RTOL
+    assert abs(np.linalg.norm(r2) - float(g["r2_norm"])) < RTOL * float(g["r2_norm"])
+
+
+def test_solve_cfg2_vs_reference(cuda, cfg2_data):
+    """Converged FP64 GPU energy within 1e-10 Eh of the reference's at no=20, nv=180."""
+    g = cfg2_data[0]
+    H = pg.Hamiltonian.from_factors(pg.SyntheticFactors(20, 180, 1, coupling="matched"), device=cuda)
+    w = pg.CCwfn(H)
+    e = w.solve_cc(1e-10, 1e-10, 100)
+    assert abs(e - float(g["ecc"])) < 1e-10
+    assert np.abs(np.array(w.energies) - g["ecc_iters"]).max() < 1e-9
+    assert rel(w.t1, g["t1"]) < 1e-7
+    wm = pg.CCwfn(H, precision="MIXED")
+    em = wm.solve_cc(1e-8, 1e-7, 100)
+    assert abs(em - float(g["ecc"])) < 1e-6

@@ -56,9 +56,32 @@ def test_solve_cc_raises_on_maxiter(cfg1_ham):
         oc.solve_cc(F, ERI, L, 5, 1e-14, 1e-14, maxiter=3)
 
 
-@pytest.mark.slow
+def probe_amplitudes(no, nv, t2_mp2, seed):
+    """Same draw as tests/golden/make_golden.py:probe_amplitudes."""
+    rng = np.random.default_rng(1000 + seed)
+    t1 = 0.02 * rng.standard_normal((no, nv))
+    noise = 0.01 * rng.standard_normal((no, no, nv, nv))
+    return t1, t2_mp2 + noise + noise.transpose(1, 0, 3, 2)
+
+
+def test_generator_cfg2_checksums():
+    from conftest import golden
+    for name, coupling in (("cfg2.npz", "matched"), ("cfg2_raw.npz", 1.0)):
+        g = golden(name)
+        fac = SyntheticFactors(20, 180, 1, coupling=coupling)
+        assert float(np.sum(fac.B * fac.B)) == pytest.approx(float(g["B_checksum"]), rel=1e-13)
+
+
 def test_residuals_cfg2_golden():
+    """The oracle's residual at no=20, nv=180 against the reference's (about a minute)."""
     from conftest import golden
     g = golden("cfg2.npz")
-    fac = SyntheticFactors(20, 180, 1)
-    assert float(np.sum(fac.B * fac.B)) == pytest.approx(float(g["B_checksum"]), rel=1e-14)
+    fac = SyntheticFactors(20, 180, 1, coupling="matched")
+    F, ERI, L = fac.hamiltonian()
+    o, v = slice(0, 20), slice(20, 200)
+    t1, t2 = probe_amplitudes(20, 180, oc.mp2_guess(F, ERI, 20)[1], 1)
+    r1, r2 = oc.residuals(o, v, F, ERI, L, t1, t2)
+    assert rel(r1, g["r1"]) < 1e-12
+    assert rel(r2[0, 1], g["r2_slice_ij01"]) < 1e-12
+    assert rel(r2[:, :, 0, 0], g["r2_slice_ab00"]) < 1e-12
+    assert np.linalg.norm(r2) == pytest.approx(float(g["r2_norm"]), rel=1e-12)
