@@ -27,7 +27,8 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int KBYTES = 128;            // bytes of K per stage row (one 128B swizzle span)
-constexpr int NT = 128;
+constexpr int NT = 192;          // warp 0: TMA, warp 1: MMA, warps 2..5: epilogue
+constexpr int EPI_THREADS = 128;
 constexpr unsigned long long kWaitNs = 4000000000ull;  // 4 s bound on any single wait
 
 enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2, kBF16x6 = 3 };
@@ -55,10 +56,12 @@ struct EpiIdx {
 
 struct Args {
   long long M, N;
-  int nkb;          // K blocks per pass in this split
-  int kb_per_split; // K blocks handled by one split (blockIdx.z)
-  int nkb_total;    // K blocks of the whole K range
-  int npass;        // 1, 3 (split-BF16x3) or 6 (split-BF16x6)
+  long long mt, nt;  // output tiles along M and N
+  int splits;        // K splits across CTAs (FP64 atomics in the epilogue when > 1)
+  int kb_per_split;  // K blocks of one split
+  int nkb_total;     // K blocks of the whole K range
+  int kb_chunk;      // K blocks accumulated in TMEM before the FP64 flush
+  int npass;         // 1, 3 (split-BF16x3) or 6 (split-BF16x6)
   PassTable pt;
   int fp8;
   EpiIdx em, en;
@@ -85,6 +88,9 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
                "r"(bytes)
                : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
@@ -179,15 +185,32 @@ struct Smem {
   static constexpr int B_BYTES = BN * KBYTES;
   static constexpr int STAGE = A_BYTES + B_BYTES;
   static constexpr int STAGES = (BN >= 256) ? 4 : (BN >= 128 ? 6 : 8);
-  static constexpr int TAIL = 1024 + BN * 8;  // barriers, tmem slot, column offsets
+  static constexpr int TAIL = 512 + 4 * BN * 8;  // barriers, tmem slot, flags, column offsets
   static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
 };
 
+// Tile t -> (split, m tile, n tile); N tiles fastest so CTAs running together share A.
+__device__ __forceinline__ void decode_tile(const Args& p, long long t, int& split, long long& m0,
+                                            long long& n0) {
+  const long long per = p.mt * p.nt;
+  split = (int)(t / per);
+  const long long r = t % per;
+  m0 = (r / p.nt) * BM;
+  n0 = (r % p.nt);
+}
+
+// Persistent, warp-specialised tcgen05 GEMM.  Each CTA walks the tiles t = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; each tile's K range is cut into chunks of kb_chunk K blocks
+// (all passes of a chunk accumulate into one TMEM buffer), and the epilogue warps add each
+// chunk's FP32 sum into the FP64 output while the MMA warp fills the other TMEM buffer.
+// Bounding the FP32 accumulation chain keeps the tensor-core accumulator's rounding
+// (truncating, so biased for long sums) at the level of a short dot product.
 template <int BN>
 __global__ void __launch_bounds__(NT, 1)
     tc_gemm_kernel(const __grid_constant__ Maps maps, const Args p) {
   using L = Smem<BN>;
   constexpr int S = L::STAGES;
+  constexpr uint32_t TMEM_COLS = 2 * BN;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -196,37 +219,35 @@ __global__ void __launch_bounds__(NT, 1)
   uint8_t* tail = base + S * L::STAGE;
   uint64_t* full = reinterpret_cast<uint64_t*>(tail);
   uint64_t* empty = full + S;
-  uint64_t* done = empty + S;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  uint64_t* tfull = empty + S;   // [2] accumulator ready (MMA -> epilogue)
+  uint64_t* tempty = tfull + 2;  // [2] accumulator drained (epilogue -> MMA)
+  uint64_t* mdone = tempty + 2;  // all MMAs of this CTA retired
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  long long* colofs = reinterpret_cast<long long*>(tail + 512);
+  long long* colofs_all = reinterpret_cast<long long*>(tail + 512);  // [4 warps][BN]
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const long long m0 = (long long)blockIdx.y * BM;
-  const long long n0 = (long long)blockIdx.x * BN;
-  const int kb0 = blockIdx.z * p.kb_per_split;
-  const int nkb = min(p.kb_per_split, p.nkb_total - kb0);
-  const int total = nkb * p.npass;
-  constexpr uint32_t TMEM_COLS = BN < 32 ? 32 : BN;
+  const long long ntiles = p.mt * p.nt * p.splits;
+  const int kelem = p.fp8 ? 128 : 64;
 
   if (tid == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(done, 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], EPI_THREADS / 32);
+    }
+    mbar_init(mdone, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
                  "r"(TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-  }
-  for (int j = tid; j < BN; j += NT) {
-    long long c = n0 + j;
-    colofs[j] = (c < p.N) ? epi_offset(p.en, c) : -1;
   }
   tc_fence_before();
   __syncthreads();
@@ -234,28 +255,40 @@ __global__ void __launch_bounds__(NT, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    if (lane == 0 && total > 0) {
+    if (lane == 0) {
       // ---- TMA producer ----
-      const uint32_t bytes = L::STAGE;
       int it = 0;
-      for (; it < total; ++it) {
-        const int s = it % S;
-        if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1)) {
-          atomicExch(p.status, kStatusTimeoutEmpty);
-          *abort_flag = 1;
-          break;
+      bool stop = false;
+      for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+        int split;
+        long long m0, nti;
+        decode_tile(p, t, split, m0, nti);
+        const int n0 = (int)(nti * BN);
+        const int kb0 = split * p.kb_per_split;
+        const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
+        for (int c0 = kb0; c0 < kb1 && !stop; c0 += p.kb_chunk) {
+          const int c1 = min(c0 + p.kb_chunk, kb1);
+          for (int pass = 0; pass < p.npass && !stop; ++pass) {
+            const CUtensorMap* ta = &maps.a[p.pt.a[pass]];
+            const CUtensorMap* tb = &maps.b[p.pt.b[pass]];
+            for (int kb = c0; kb < c1; ++kb, ++it) {
+              const int s = it % S;
+              if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1)) {
+                atomicExch(p.status, kStatusTimeoutEmpty);
+                *abort_flag = 1;
+              }
+              if (*abort_flag) {
+                stop = true;
+                break;
+              }
+              mbar_expect_tx(&full[s], L::STAGE);
+              tma_load_2d(ta, &full[s], sA + s * L::A_BYTES, kb * kelem, (int)m0);
+              tma_load_2d(tb, &full[s], sB + s * L::B_BYTES, kb * kelem, n0);
+            }
+          }
         }
-        if (*abort_flag) break;
-        const int pass = it / nkb;
-        const int kb = kb0 + (it % nkb);
-        const CUtensorMap* ta = &maps.a[p.pt.a[pass]];
-        const CUtensorMap* tb = &maps.b[p.pt.b[pass]];
-        const int kx = kb * (p.fp8 ? 128 : 64);
-        mbar_expect_tx(&full[s], bytes);
-        tma_load_2d(ta, &full[s], sA + s * L::A_BYTES, kx, (int)m0);
-        tma_load_2d(tb, &full[s], sB + s * L::B_BYTES, kx, (int)n0);
       }
-      if (*abort_flag) {
+      if (stop) {
         // let the copies already in flight land before the CTA releases its shared memory
         for (int j = max(0, it - S); j < it; ++j) mbar_wait(&full[j % S], (j / S) & 1);
       }
@@ -266,67 +299,129 @@ __global__ void __launch_bounds__(NT, 1)
       // ---- MMA issuer ----
       uint32_t idesc = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
       if (!p.fp8) idesc |= (1u << 7) | (1u << 10);  // A, B = BF16 (FP8 E4M3 encodes as 0)
-      for (int it = 0; it < total; ++it) {
-        const int s = it % S;
-        if (!mbar_wait(&full[s], (it / S) & 1)) {
-          atomicExch(p.status, kStatusTimeoutFull);
-          *abort_flag = 1;
-          break;
-        }
-        if (*abort_flag) break;
-        tc_fence_after();
-        const uint64_t da = sw128_desc(smem_u32(sA + s * L::A_BYTES));
-        const uint64_t db = sw128_desc(smem_u32(sB + s * L::B_BYTES));
+      int it = 0, u = 0;
+      bool stop = false;
+      for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+        int split;
+        long long m0, nti;
+        decode_tile(p, t, split, m0, nti);
+        const int kb0 = split * p.kb_per_split;
+        const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
+        for (int c0 = kb0; c0 < kb1 && !stop; c0 += p.kb_chunk, ++u) {
+          const int c1 = min(c0 + p.kb_chunk, kb1);
+          const int b = u & 1;
+          if (u >= 2 && !mbar_wait(&tempty[b], ((u >> 1) - 1) & 1)) {
+            atomicExch(p.status, kStatusTimeoutEmpty);
+            *abort_flag = 1;
+          }
+          if (*abort_flag) {
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + (uint32_t)(b * BN);
+          uint32_t acc = 0u;
+          for (int pass = 0; pass < p.npass && !stop; ++pass) {
+            for (int kb = c0; kb < c1; ++kb, ++it) {
+              const int s = it % S;
+              if (!mbar_wait(&full[s], (it / S) & 1)) {
+                atomicExch(p.status, kStatusTimeoutFull);
+                *abort_flag = 1;
+              }
+              if (*abort_flag) {
+                stop = true;
+                break;
+              }
+              tc_fence_after();
+              const uint64_t da = sw128_desc(smem_u32(sA + s * L::A_BYTES));
+              const uint64_t db = sw128_desc(smem_u32(sB + s * L::B_BYTES));
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per 128-byte stage row
-          const uint32_t acc = (it > 0 || k > 0) ? 1u : 0u;
-          if (p.fp8)
-            umma_f8(tmem, da + 2 * k, db + 2 * k, idesc, acc);
-          else
-            umma_f16(tmem, da + 2 * k, db + 2 * k, idesc, acc);
+              for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per 128-byte stage row
+                if (p.fp8)
+                  umma_f8(d, da + 2 * k, db + 2 * k, idesc, acc);
+                else
+                  umma_f16(d, da + 2 * k, db + 2 * k, idesc, acc);
+                acc = 1u;
+              }
+              umma_commit(&empty[s]);
+            }
+          }
+          umma_commit(&tfull[b]);
         }
-        umma_commit(&empty[s]);
       }
-      umma_commit(done);
+      umma_commit(mdone);
+      mbar_wait(mdone, 0);  // every MMA of this CTA has retired before TMEM is released
     }
     __syncwarp();
-  }
-
-  // ---- epilogue: TMEM -> registers -> FP64 C ----
-  bool ok = (total > 0) ? mbar_wait(done, 0) : false;
-  if (!ok && total > 0) atomicExch(p.status, kStatusTimeoutDone);
-  __syncwarp();
-  tc_fence_after();
-  ok = ok && (*abort_flag == 0);
-  const long long row = m0 + warp * 32 + lane;
-  const bool row_ok = row < p.M;
-  const long long roff = row_ok ? epi_offset(p.em, row) : 0;
-  const double ascale = (p.fp8 && row_ok) ? (double)p.a_scale[row] : 1.0;
-  if (ok) {
+  } else {
+    // ---- epilogue warps: TMEM -> registers -> FP64 C, one chunk at a time ----
+    const int q = warp & 3;  // the TMEM lane quarter this warp may read
+    long long* colofs = colofs_all + (warp - 2) * BN;  // this warp's copy
+    int u = 0;
+    bool stop = false;
+    for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+      int split;
+      long long m0, nti;
+      decode_tile(p, t, split, m0, nti);
+      const long long n0 = nti * BN;
+      const int kb0 = split * p.kb_per_split;
+      const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
+      const long long row = m0 + q * 32 + lane;
+      const bool row_ok = row < p.M;
+      const long long roff = row_ok ? epi_offset(p.em, row) : 0;
+      const double ascale = (p.fp8 && row_ok) ? (double)p.a_scale[row] : 1.0;
+      __syncwarp();  // the previous tile's column offsets are no longer read
+      for (int j = lane; j < BN; j += 32) {
+        const long long c = n0 + j;
+        colofs[j] = (c < p.N) ? epi_offset(p.en, c) : -1;
+      }
+      __syncwarp();
+      bool first = true;
+      for (int c0 = kb0; c0 < kb1; c0 += p.kb_chunk, ++u) {
+        const int b = u & 1;
+        const bool ok = mbar_wait(&tfull[b], (u >> 1) & 1);
+        if (!ok) {
+          atomicExch(p.status, kStatusTimeoutDone);
+          *abort_flag = 1;
+        }
+        // warp-uniform decision: tcgen05.ld below is a .sync.aligned warp instruction
+        if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) {
+          stop = true;
+          break;
+        }
+        tc_fence_after();
 #pragma unroll 1
-    for (int c0 = 0; c0 < BN; c0 += 32) {
-      uint32_t r[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, r);
-      if (!row_ok) continue;
+        for (int cc = 0; cc < BN; cc += 32) {
+          uint32_t r[32];
+          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + cc), r);
+          if (!row_ok) continue;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const long long co = colofs[c0 + j];
-        if (co < 0) continue;
-        double v = (double)__uint_as_float(r[j]) * p.alpha;
-        if (p.fp8) v *= ascale * (double)p.b_scale[n0 + c0 + j];
-        double* dst = p.C + roff + co;
-        if (p.atomic_out)
-          atomicAdd(dst, v);
-        else if (p.beta == 0.0)
-          *dst = v;
-        else
-          *dst = p.beta * *dst + v;
+          for (int j = 0; j < 32; ++j) {
+            const long long co = colofs[cc + j];
+            if (co < 0) continue;
+            double v = (double)__uint_as_float(r[j]) * p.alpha;
+            if (p.fp8) v *= ascale * (double)p.b_scale[n0 + cc + j];
+            double* dst = p.C + roff + co;
+            if (p.atomic_out)
+              atomicAdd(dst, v);
+            else if (!first)
+              *dst += v;
+            else if (p.beta == 0.0)
+              *dst = v;
+            else
+              *dst = p.beta * *dst + v;
+          }
+        }
+        first = false;
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&tempty[b]);
       }
     }
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS));
@@ -496,16 +591,17 @@ int num_sms() {
 }
 
 template <int BN>
-int launch(const Maps& maps, const Args& a, long long mt, long long nt, int splits,
-           cudaStream_t st) {
+int launch(const Maps& maps, Args a, cudaStream_t st) {
   static bool attr = false;
   const int smem = Smem<BN>::TOTAL;
   if (!attr) {
     cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  dim3 grid((unsigned)nt, (unsigned)mt, (unsigned)splits);
-  tc_gemm_kernel<BN><<<grid, NT, smem, st>>>(maps, a);
+  a.nt = (a.N + BN - 1) / BN;
+  const long long ntiles = a.mt * a.nt * a.splits;
+  const long long grid = std::min<long long>(ntiles, num_sms());
+  tc_gemm_kernel<BN><<<(unsigned)grid, NT, smem, st>>>(maps, a);
   PCG_CHECK_LAUNCH("pcg_tc_gemm");
   return 0;
 }
@@ -655,8 +751,8 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.status = status;
   const int BN = (N <= 64) ? 64 : (N <= 128 ? 128 : 256);
   long long mt = (M + BM - 1) / BM, nt = (N + BN - 1) / BN;
-  if (mt > 65535 || nt > 0x7fffffffLL) {
-    set_error("pcg_tc_gemm: grid too large (M tiles %lld)", mt);
+  if (mt > 0x7fffffffLL || nt > 0x7fffffffLL) {
+    set_error("pcg_tc_gemm: too many tiles (M tiles %lld)", mt);
     return -1;
   }
   const int nkb = (int)(Kp / kblk);
@@ -669,8 +765,13 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   }
   int kps = (nkb + splits - 1) / splits;
   splits = (nkb + kps - 1) / kps;
+  a.mt = mt;
+  a.nt = nt;
+  a.splits = splits;
   a.nkb_total = nkb;
   a.kb_per_split = kps;
+  // FP32 accumulation chain per flush: 4096 K for split-BF16x3, 2048 for BF16x6
+  a.kb_chunk = (fmt == kBF16x3) ? 64 : (fmt == kBF16x6 ? 32 : 192);
   a.atomic_out = splits > 1;
   cudaStream_t st = (cudaStream_t)stream;
   if (a.atomic_out && beta != 1.0) {
@@ -686,8 +787,8 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
     if (!make_map(&maps.b[q], pb[q] ? pb[q] : B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
   }
   switch (BN) {
-    case 64: return launch<64>(maps, a, mt, nt, splits, st);
-    case 128: return launch<128>(maps, a, mt, nt, splits, st);
-    default: return launch<256>(maps, a, mt, nt, splits, st);
+    case 64: return launch<64>(maps, a, st);
+    case 128: return launch<128>(maps, a, st);
+    default: return launch<256>(maps, a, st);
   }
 }

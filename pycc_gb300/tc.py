@@ -201,8 +201,16 @@ class TCEngine:
         kk.sort(key=lambda c: -dst[c])
         mA = math.prod(ea[c] for c in ma) if ma else 1
         nB = math.prod(eb[c] for c in nb) if nb else 1
-        # the larger free dimension takes the 128-row tile side
-        if nB > mA:
+        # The 128-row tile side: the side holding the output's unit-stride index (so a warp's
+        # 32 consecutive rows store to consecutive addresses), unless it is too short.
+        inner = min(rhs, key=lambda c: abs(ost[c]))
+        if inner in nb and nB >= 128:
+            swap = True
+        elif inner in ma and mA >= 128:
+            swap = False
+        else:
+            swap = nB > mA
+        if swap:
             A, B, ma, nb = B, A, nb, ma
         pa = self._pack(A, ma, kk, fmt, "A")
         pb = self._pack(B, nb, kk, fmt, "B")
