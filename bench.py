@@ -235,6 +235,7 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     modes = w.mixed_engine().history[-args.steps:]
+    iter_ms = [round(x * 1e3, 2) for x in w.iter_times[-args.steps:]]
     timed_energy = w.energies[-1]
     # iterate on (untimed) to the precision floor for the converged mixed energy
     e_mixed = None
@@ -344,7 +345,7 @@ def main():
                    "coupling": "matched (lambda=%.4f)" % fac.coupling,
                    "l2": "inputs larger than L2 (integral blocks ~%.0f GB)" % (H.nbytes() / 1e9),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "s_per_iter": ms * 1e-3, "modes_timed": modes, "energy_timed_last": timed_energy,
+        "s_per_iter": ms * 1e-3, "modes_timed": modes, "iter_wall_ms": iter_ms, "energy_timed_last": timed_energy,
         "energy_mixed": e_mixed, "energy_error_vs_fp64": err,
         "fp64": fp64, "roofline": roofline, "cpu_baseline": cpu,
         "e2e": {"value": F_it / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",

@@ -112,6 +112,19 @@ __device__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     if (gtimer() - t0 > kWaitNs) return false;
   }
 }
+// Bounded wait with nanosleep back-off, for threads off the critical issue path.
+__device__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  unsigned long long t0 = gtimer();
+  unsigned ns = 32;
+  for (;;) {
+    for (int i = 0; i < 8; ++i)
+      if (mbar_try(bar, parity)) return true;
+    __nanosleep(ns);
+    if (ns < 256) ns <<= 1;
+    if (gtimer() - t0 > kWaitNs) return false;
+  }
+}
 __device__ __forceinline__ void tma_load_2d(const CUtensorMap* tm, uint64_t* bar, void* dst, int x,
                                             int y) {
   asm volatile(
@@ -379,37 +392,46 @@ __global__ void __launch_bounds__(NT, 1)
       bool first = true;
       for (int c0 = kb0; c0 < kb1; c0 += p.kb_chunk, ++u) {
         const int b = u & 1;
-        const bool ok = mbar_wait(&tfull[b], (u >> 1) & 1);
-        if (!ok) {
-          atomicExch(p.status, kStatusTimeoutDone);
-          *abort_flag = 1;
+        // one lane polls (with back-off), the warp follows
+        int okw = 1;
+        if (lane == 0) {
+          okw = mbar_wait_sleep(&tfull[b], (u >> 1) & 1) ? 1 : 0;
+          if (!okw) {
+            atomicExch(p.status, kStatusTimeoutDone);
+            *abort_flag = 1;
+          }
+          if (*abort_flag) okw = 0;
         }
         // warp-uniform decision: tcgen05.ld below is a .sync.aligned warp instruction
-        if (__any_sync(0xffffffffu, !ok || *abort_flag != 0)) {
+        if (!__shfl_sync(0xffffffffu, okw, 0)) {
           stop = true;
           break;
         }
         tc_fence_after();
+        const double cscale = first ? p.beta : 1.0;  // beta applies once per tile
+        const bool need_old = !p.atomic_out && cscale != 0.0;
+        double* crow = p.C + roff;
 #pragma unroll 1
         for (int cc = 0; cc < BN; cc += 32) {
           uint32_t r[32];
           tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + cc), r);
           if (!row_ok) continue;
+          long long co[32];
+          double old[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) co[j] = colofs[cc + j];
+          // all loads of the batch before any store: 32 independent requests in flight
+#pragma unroll
+          for (int j = 0; j < 32; ++j) old[j] = (need_old && co[j] >= 0) ? crow[co[j]] : 0.0;
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            const long long co = colofs[cc + j];
-            if (co < 0) continue;
+            if (co[j] < 0) continue;
             double v = (double)__uint_as_float(r[j]) * p.alpha;
             if (p.fp8) v *= ascale * (double)p.b_scale[n0 + cc + j];
-            double* dst = p.C + roff + co;
             if (p.atomic_out)
-              atomicAdd(dst, v);
-            else if (!first)
-              *dst += v;
-            else if (p.beta == 0.0)
-              *dst = v;
+              atomicAdd(crow + co[j], v);
             else
-              *dst = p.beta * *dst + v;
+              crow[co[j]] = cscale * old[j] + v;
           }
         }
         first = false;
