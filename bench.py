@@ -176,6 +176,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-terms", action="store_true")
+    ap.add_argument("--force-mode", default=None, choices=[None, "bf16x3"],
+                    help="start in the final precision stage (profiling of that stage)")
+    ap.add_argument("--converge-iters", type=int, default=60,
+                    help="untimed iterations allowed after the timed ones to reach the floor")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -206,6 +210,8 @@ def main():
 
     # ---- mixed-precision solve: W warm-up + K timed iterations ----------------------------
     w = pg.CCwfn(H, precision="MIXED")
+    if args.force_mode:
+        w.mixed_engine().force_final()
     diis = w.start_iterations(8)
     n = 0
     for _ in range(args.warmup):
@@ -239,7 +245,7 @@ def main():
     timed_energy = w.energies[-1]
     # iterate on (untimed) to the precision floor for the converged mixed energy
     e_mixed = None
-    for _ in range(60):
+    for _ in range(args.converge_iters):
         if w.mixed_engine().at_floor():
             e_mixed = float(np.mean(w.energies[-4:]))
             break
@@ -290,14 +296,15 @@ def main():
         r2h.copy_(r2, non_blocking=True)
         torch.cuda.current_stream().synchronize()
 
-    e2e_step()
+    if args.e2e_steps > 0:
+        e2e_step()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(args.e2e_steps):
         e2e_step()
     e1.record()
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+    e2e_ms = e0.elapsed_time(e1) / max(args.e2e_steps, 1)
     nb = (t1h.numel() + t2h.numel()) * 8
 
     # ---- plain FP64 form at the same size --------------------------------------------------
