@@ -195,6 +195,46 @@ __global__ void contract_gemv_kernel(const F64Args p) {
   }
 }
 
+// Matrix-vector shapes whose operand B is unit-stride along the output's innermost
+// sub-index: one thread per output, consecutive threads on consecutive outputs (coalesced
+// B reads); the K offsets are staged in shared memory once per block.
+__global__ void __launch_bounds__(256) contract_gemv_thread_kernel(const F64Args p) {
+  __shared__ long long ka[256], kb[256];
+  const long long o = (long long)blockIdx.x * 256 + threadIdx.x;
+  const bool valid = o < p.M * p.N;
+  long long am = 0, cm = 0, bn = 0, cn = 0;
+  if (valid) {
+    sub_offsets(p.m, o / p.N, am, cm);
+    sub_offsets(p.n, o % p.N, bn, cn);
+  }
+  double acc = 0.0;
+  for (long long k0 = 0; k0 < p.K; k0 += 256) {
+    __syncthreads();
+    const long long k = k0 + threadIdx.x;
+    if (k < p.K) sub_offsets(p.k, k, ka[threadIdx.x], kb[threadIdx.x]);
+    __syncthreads();
+    const int kn = (int)min((long long)256, p.K - k0);
+    if (valid)
+      for (int j = 0; j < kn; ++j) acc += p.A[am + ka[j]] * p.B[bn + kb[j]];
+  }
+  if (valid) {
+    double* dst = p.C + cm + cn;
+    const double v = p.alpha * acc;
+    *dst = (p.beta == 0.0) ? v : p.beta * *dst + v;
+  }
+}
+
+// Reorder sub-indices by decreasing |stride| in the operand (s0), unit stride innermost.
+void sort_by_operand_stride(SubIdx& d) {
+  for (int i = 0; i < d.n; ++i)
+    for (int j = i + 1; j < d.n; ++j)
+      if (llabs(d.s0[j]) > llabs(d.s0[i])) {
+        std::swap(d.ext[i], d.ext[j]);
+        std::swap(d.s0[i], d.s0[j]);
+        std::swap(d.s1[i], d.s1[j]);
+      }
+}
+
 bool fill_sub(SubIdx& d, int n, const long long* ext, const long long* s0, const long long* s1,
               const char* what) {
   if (n < 0 || n > kMaxSub) {
@@ -261,6 +301,25 @@ extern "C" int pcg_contract_f64(int m_n, const long long* m_ext, const long long
   p.a_kfast = (p.k.s0[p.k.n - 1] == 1) ? 1 : 0;
   p.b_kfast = (p.k.s1[p.k.n - 1] == 1) ? 1 : 0;
   cudaStream_t st = (cudaStream_t)stream;
+  if (p.M == 1 || p.N == 1) {
+    // one free side: enumerate the outputs along the big operand's unit-stride index
+    F64Args q = p;
+    if (q.M == 1) {
+      sort_by_operand_stride(q.n);
+    } else {  // N == 1: swap roles so the free index is on the B side
+      std::swap(q.m, q.n);
+      std::swap(q.M, q.N);
+      std::swap(q.A, q.B);
+      for (int i = 0; i < q.k.n; ++i) std::swap(q.k.s0[i], q.k.s1[i]);
+      sort_by_operand_stride(q.n);
+    }
+    if (q.n.s0[q.n.n - 1] == 1 && q.M * q.N >= 1024) {
+      const long long blocks = (q.M * q.N + 255) / 256;
+      contract_gemv_thread_kernel<<<(unsigned)blocks, 256, 0, st>>>(q);
+      PCG_CHECK_LAUNCH("pcg_contract_f64/gemv_thread");
+      return 0;
+    }
+  }
   if (p.M < 8 || p.N < 8) {
     long long warps = p.M * p.N;
     int blocks = (int)std::min<long long>((warps * 32 + 255) / 256, 152LL * 64);

@@ -497,57 +497,112 @@ __device__ __forceinline__ double pack_value(const PackArgs& p, const long long 
   return v;
 }
 
-// One CTA per row; BF16 / split-BF16 outputs.
-__global__ void pack_bf16_kernel(const PackArgs p) {
-  const long long r = blockIdx.x + (long long)blockIdx.y * 65535;
-  if (r >= p.R) return;
-  long long ro[4];
-  pack_offsets(p.r, r, ro);
-  __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(p.hi) + r * p.Kp;
-  __nv_bfloat16* lo = p.lo ? reinterpret_cast<__nv_bfloat16*>(p.lo) + r * p.Kp : nullptr;
-  __nv_bfloat16* mid = p.mid ? reinterpret_cast<__nv_bfloat16*>(p.mid) + r * p.Kp : nullptr;
-  for (long long k = threadIdx.x; k < p.Kp; k += blockDim.x) {
-    double v = (k < p.K) ? pack_value(p, ro, k) : 0.0;
-    __nv_bfloat16 h = __double2bfloat16(v);
-    hi[k] = h;
+// Tiled pack: a block handles TR rows x TK columns of K.  Row and column offsets of the
+// four sources are decomposed once per tile into shared memory; values are gathered along
+// whichever index is unit-stride in X (kfast) and written out along K, so both the FP64
+// reads and the packed writes are coalesced.
+constexpr int TR = 32, TK = 64, PACK_THREADS = 256;
+
+struct PackTile {
+  long long rof[4][TR];
+  long long kof[4][TK];
+  double v[TR][TK + 1];
+};
+
+__device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile& t, long long r0,
+                                               long long k0, int kfast) {
+  const int tid = threadIdx.x;
+  if (tid < TR) {
+    long long o[4] = {0, 0, 0, 0};
+    if (r0 + tid < p.R) pack_offsets(p.r, r0 + tid, o);
+    for (int s = 0; s < 4; ++s) t.rof[s][tid] = o[s];
+  } else if (tid >= 64 && tid < 64 + TK) {
+    const int j = tid - 64;
+    long long o[4] = {0, 0, 0, 0};
+    if (k0 + j < p.K) pack_offsets(p.k, k0 + j, o);
+    for (int s = 0; s < 4; ++s) t.kof[s][j] = o[s];
+  }
+  __syncthreads();
+  for (int e = tid; e < TR * TK; e += PACK_THREADS) {
+    int rr, kk;
+    if (kfast) { rr = e / TK; kk = e % TK; } else { kk = e / TR; rr = e % TR; }
+    double v = 0.0;
+    if (r0 + rr < p.R && k0 + kk < p.K) {
+      v = p.X ? p.a * p.X[t.rof[0][rr] + t.kof[0][kk]] : 0.0;
+      if (p.Y) v += p.b * p.Y[t.rof[1][rr] + t.kof[1][kk]];
+      if (p.P) v += p.c * p.P[t.rof[2][rr] + t.kof[2][kk]] * p.Q[t.rof[3][rr] + t.kof[3][kk]];
+    }
+    t.v[rr][kk] = v;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs p, int kfast) {
+  __shared__ PackTile t;
+  const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
+  pack_tile_load(p, t, r0, k0, kfast);
+  __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(p.hi);
+  __nv_bfloat16* mid = reinterpret_cast<__nv_bfloat16*>(p.mid);
+  __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(p.lo);
+  for (int e = threadIdx.x; e < TR * TK; e += PACK_THREADS) {
+    const int rr = e / TK, kk = e % TK;
+    if (r0 + rr >= p.R) continue;
+    const long long at = (r0 + rr) * p.Kp + k0 + kk;
+    const double v = t.v[rr][kk];
+    const __nv_bfloat16 h = __double2bfloat16(v);
+    hi[at] = h;
     double rest = v - (double)__bfloat162float(h);
     if (mid) {
-      __nv_bfloat16 m = __double2bfloat16(rest);
-      mid[k] = m;
+      const __nv_bfloat16 m = __double2bfloat16(rest);
+      mid[at] = m;
       rest -= (double)__bfloat162float(m);
     }
-    if (lo) lo[k] = __double2bfloat16(rest);
+    if (lo) lo[at] = __double2bfloat16(rest);
   }
 }
 
-// One CTA per row; FP8 E4M3 with a per-row scale (row absmax / 448).
-__global__ void pack_fp8_kernel(const PackArgs p) {
-  const long long r = blockIdx.x + (long long)blockIdx.y * 65535;
-  if (r >= p.R) return;
-  long long ro[4];
-  pack_offsets(p.r, r, ro);
-  double m = 0.0;
-  for (long long k = threadIdx.x; k < p.K; k += blockDim.x) m = fmax(m, fabs(pack_value(p, ro, k)));
-  __shared__ double red[32];
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    m = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+// FP8 pass 1: per-row max |v| into rowmax (float bits, zero-initialised; |v| >= 0 so the
+// unsigned order of the bits is the float order).
+__global__ void __launch_bounds__(PACK_THREADS) pack_fp8_max_kernel(const PackArgs p, int kfast,
+                                                                    unsigned* rowmax) {
+  __shared__ PackTile t;
+  const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
+  pack_tile_load(p, t, r0, k0, kfast);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int rr = warp; rr < TR; rr += PACK_THREADS / 32) {
+    double m = fmax(fabs(t.v[rr][lane]), fabs(t.v[rr][lane + 32]));
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (threadIdx.x == 0) red[0] = m;
+    if (lane == 0 && r0 + rr < p.R && m > 0.0)
+      atomicMax(rowmax + r0 + rr, __float_as_uint((float)m));
   }
-  __syncthreads();
-  m = red[0];
-  // power-of-two scale: the smallest 2^e with max|v| / 2^e <= 448, so dequantisation is exact
-  const double s = (m > 0.0) ? exp2(ceil(log2(m / 448.0))) : 1.0;
-  if (threadIdx.x == 0) p.scale[r] = (float)s;
-  const double inv = 1.0 / s;
-  __nv_fp8_e4m3* dst = reinterpret_cast<__nv_fp8_e4m3*>(p.hi) + r * p.Kp;
-  for (long long k = threadIdx.x; k < p.Kp; k += blockDim.x) {
-    double v = (k < p.K) ? pack_value(p, ro, k) * inv : 0.0;
-    dst[k] = __nv_fp8_e4m3((float)v);
+}
+
+__device__ __forceinline__ double fp8_scale(unsigned maxbits) {
+  // smallest power of two 2^e with max|v| / 2^e <= 448, so dequantisation is exact
+  const double m = (double)__uint_as_float(maxbits);
+  return (m > 0.0) ? exp2(ceil(log2(m / 448.0))) : 1.0;
+}
+
+// FP8 pass 2: quantise with the row's power-of-two scale.
+__global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p, int kfast,
+                                                                const unsigned* rowmax) {
+  __shared__ PackTile t;
+  const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
+  pack_tile_load(p, t, r0, k0, kfast);
+  __nv_fp8_e4m3* dst = reinterpret_cast<__nv_fp8_e4m3*>(p.hi);
+  for (int e = threadIdx.x; e < TR * TK; e += PACK_THREADS) {
+    const int rr = e / TK, kk = e % TK;
+    if (r0 + rr >= p.R) continue;
+    const double inv = 1.0 / fp8_scale(rowmax[r0 + rr]);
+    dst[(r0 + rr) * p.Kp + k0 + kk] = __nv_fp8_e4m3((float)(t.v[rr][kk] * inv));
   }
+}
+
+// FP8 pass 3: replace each row's max bits by its scale.
+__global__ void pack_fp8_scale_kernel(long long R, unsigned* rowmax_scale) {
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < R;
+       r += (long long)gridDim.x * blockDim.x)
+    reinterpret_cast<float*>(rowmax_scale)[r] = (float)fp8_scale(rowmax_scale[r]);
 }
 
 __global__ void scale_epi_kernel(EpiIdx em, EpiIdx en, long long M, long long N, double beta,
@@ -710,12 +765,31 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   p.mid = (fmt == kBF16x6) ? mid : nullptr;
   p.scale = row_scale;
   p.fmt = fmt;
-  dim3 grid((unsigned)std::min<long long>(p.R, 65535), (unsigned)((p.R + 65534) / 65535));
+  // gather along K when X is at least as contiguous along K as along the rows
+  long long ks = 0, rs = 0;
+  for (int q = 0; q < p.k.n; ++q)
+    if (p.k.s[0][q] != 0) ks = (ks == 0) ? llabs(p.k.s[0][q]) : std::min(ks, llabs(p.k.s[0][q]));
+  for (int q = 0; q < p.r.n; ++q)
+    if (p.r.s[0][q] != 0) rs = (rs == 0) ? llabs(p.r.s[0][q]) : std::min(rs, llabs(p.r.s[0][q]));
+  const int kfast = (rs == 0 || (ks != 0 && ks <= rs)) ? 1 : 0;
+  const long long gx = (p.R + TR - 1) / TR, gy = Kp / TK;
+  if (gy > 65535 || gx > 0x7fffffffLL) {
+    set_error("pcg_pack_operand: operand too large (%lld x %lld)", p.R, Kp);
+    return -1;
+  }
+  dim3 grid((unsigned)gx, (unsigned)gy);
   cudaStream_t st = (cudaStream_t)stream;
-  if (fmt == kFP8)
-    pack_fp8_kernel<<<grid, 256, 0, st>>>(p);
-  else
-    pack_bf16_kernel<<<grid, 256, 0, st>>>(p);
+  if (fmt == kFP8) {
+    unsigned* mx = reinterpret_cast<unsigned*>(row_scale);
+    cudaMemsetAsync(mx, 0, sizeof(float) * p.R, st);
+    pack_fp8_max_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, mx);
+    PCG_CHECK_LAUNCH("pcg_pack_operand/max");
+    pack_fp8_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, mx);
+    PCG_CHECK_LAUNCH("pcg_pack_operand/fp8");
+    pack_fp8_scale_kernel<<<(unsigned)std::min<long long>((p.R + 255) / 256, 4096), 256, 0, st>>>(p.R, mx);
+  } else {
+    pack_bf16_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast);
+  }
   PCG_CHECK_LAUNCH("pcg_pack_operand");
   return 0;
 }

@@ -6,7 +6,7 @@ from pycc_gb300.contract import contract_f64
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = {"o": 5, "v": 19}
+SHAPES = {"o": 5, "v": 37}
 TERMS = [
     ("mnaf,mnef->ae", "oovv", "oovv"), ("ijef,mnef->mnij", "oovv", "oovv"),
     ("jf,mbef->mbej", "ov", "ovvv"), ("jnfb,mnef->mbej", "oovv", "oovv"),
@@ -15,6 +15,9 @@ TERMS = [
     ("ijef,abef->ijab", "oovv", "vvvv"), ("imae,mbej->ijab", "oovv", "ovvo"),
     ("mjae,mbie->ijab", "oovv", "ovov"), ("ie,ma->imea", "ov", "ov"),
     ("ie,abej->ijab", "ov", "vvvo"), ("ia,ia->", "ov", "ov"),
+    # matrix-vector shapes (thread- and warp-per-output paths)
+    ("mf,mafe->ae", "ov", "ovvv"), ("nf,nafi->ia", "ov", "ovvo"), ("nf,mnef->me", "ov", "oovv"),
+    ("imae,me->ia", "oovv", "ov"), ("mafe,mf->ae", "ovvv", "ov"),
 ]
 
 
