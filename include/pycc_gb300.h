@@ -72,6 +72,14 @@ int pcg_energy_f64(const double* fov, const long long* fs2, const double* L,
 int pcg_dots_f64(const double* x, const double* const* ys, int k, long long n, double* work,
                  long long work_len, double* out, void* stream);
 
+/* e = x - old (e written; e must not alias x or old) and, in the same pass,
+ * out[j] = <e, ys[j]> for j < k-1 and out[k-1] = <e, e>; 1 <= k <= 16 (ys: host array of
+ * k-1 device pointers); work >= 1024*k doubles.  helper_diis.add_error_vector and the
+ * overlap matrix of helper_diis.extrapolate (pycc/utils.py:284-295, :330-339) */
+int pcg_diis_error_f64(const double* x, const double* old, double* e, const double* const* ys,
+                       int k, long long n, double* work, long long work_len, double* out,
+                       void* stream);
+
 /* out = sum_j c[j]*xs[j], 1 <= k <= 16 (xs, c on the host; out must not alias an input).
  * DIIS extrapolation, helper_diis.extrapolate (pycc/utils.py:351-355) */
 int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n, double* out,

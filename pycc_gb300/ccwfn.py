@@ -362,7 +362,7 @@ class CCwfn:
     def diis_step(self, diis, niter, start_diis=1):
         diis.add_error_vector(self._amps)
         if niter >= start_diis:
-            self._amps.copy_(diis.extrapolate(self._amps))
+            diis.extrapolate(self._amps)       # in place
 
     def solve_cc(self, e_conv=1e-7, r_conv=1e-7, maxiter=100, max_diis=8, start_diis=1,
                  callback=None):

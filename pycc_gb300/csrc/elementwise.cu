@@ -172,6 +172,29 @@ __global__ void dots_kernel(const double* __restrict__ x, VecList ys, int k, lon
   }
 }
 
+// e = x - old (written) and part[j] = <e, ys[j]> for j < k-1, part[k-1] = <e, e>.
+__global__ void diis_error_kernel(const double* __restrict__ x, const double* __restrict__ old,
+                                  double* __restrict__ e, VecList ys, int k, long long n,
+                                  double* __restrict__ part) {
+  double acc[kMaxVec];
+#pragma unroll
+  for (int j = 0; j < kMaxVec; ++j) acc[j] = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double ev = x[idx] - old[idx];
+    e[idx] = ev;
+#pragma unroll
+    for (int j = 0; j < kMaxVec - 1; ++j)
+      if (j < k - 1) acc[j] += ev * ys.p[j][idx];
+    acc[kMaxVec - 1] += ev * ev;
+  }
+  for (int j = 0; j < k; ++j) {
+    double v = block_sum(j == k - 1 ? acc[kMaxVec - 1] : acc[j]);
+    if (threadIdx.x == 0) part[(long long)j * gridDim.x + blockIdx.x] = v;
+    __syncthreads();
+  }
+}
+
 __global__ void lincomb_kernel(VecList xs, int k, long long n, double* __restrict__ out) {
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
        idx += (long long)gridDim.x * blockDim.x) {
@@ -312,5 +335,28 @@ extern "C" int pcg_lincomb_f64(const double* const* xs, const double* c, int k, 
   }
   lincomb_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(v, k, n, out);
   PCG_CHECK_LAUNCH("pcg_lincomb_f64");
+  return 0;
+}
+
+extern "C" int pcg_diis_error_f64(const double* x, const double* old, double* e,
+                                  const double* const* ys, int k, long long n, double* work,
+                                  long long work_len, double* out, void* stream) {
+  if (k < 1 || k > kMaxVec) {
+    set_error("pcg_diis_error_f64: k=%d outside [1, %d]", k, kMaxVec);
+    return -1;
+  }
+  if (!x || !old || !e || e == x || e == old) {
+    set_error("pcg_diis_error_f64: bad pointers");
+    return -1;
+  }
+  if (!check_work(work_len, (long long)k * RED_BLOCKS, "pcg_diis_error_f64")) return -1;
+  cudaStream_t st = (cudaStream_t)stream;
+  VecList v{};
+  for (int j = 0; j + 1 < k; ++j) v.p[j] = ys[j];
+  int nb = std::min(ew_blocks(n), RED_BLOCKS);
+  diis_error_kernel<<<nb, EW_THREADS, 0, st>>>(x, old, e, v, k, n, work);
+  PCG_CHECK_LAUNCH("pcg_diis_error_f64/partials");
+  finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, k, out);
+  PCG_CHECK_LAUNCH("pcg_diis_error_f64");
   return 0;
 }

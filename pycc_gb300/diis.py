@@ -33,19 +33,16 @@ class DIIS:
 
     def add_error_vector(self, amps: torch.Tensor):
         self.vals.append(amps.clone())
+        k = len(self.errors) + 1
         e = torch.empty_like(amps)
-        n = amps.numel()
-        ext = _lib.i64s([1, 1, 1, n])
-        unit = _lib.i64s([0, 0, 0, 1])
-        _lib.call("pcg_combine4_f64", ext, 1.0, amps.data_ptr(), unit, -1.0, self.old.data_ptr(),
-                  unit, e.data_ptr(), unit, _lib.stream_handle(self.stream))
+        # e = amps - old, written once, and its overlaps with every stored error vector
+        # (itself included) in the same pass
+        ptrs = (C.c_void_p * k)(*([x.data_ptr() for x in self.errors] + [0]))
+        _lib.call("pcg_diis_error_f64", amps.data_ptr(), self.old.data_ptr(), e.data_ptr(), ptrs,
+                  k, e.numel(), self.work.data_ptr(), self.work.numel(), self.dots.data_ptr(),
+                  _lib.stream_handle(self.stream))
         self.errors.append(e)
-        self.old = amps.clone()
-        k = len(self.errors)
-        # overlaps of the new vector with every stored one (itself included)
-        ptrs = (C.c_void_p * k)(*[x.data_ptr() for x in self.errors])
-        _lib.call("pcg_dots_f64", e.data_ptr(), ptrs, k, e.numel(), self.work.data_ptr(),
-                  self.work.numel(), self.dots.data_ptr(), _lib.stream_handle(self.stream))
+        self.old = self.vals[-1]          # the stored copy of the current amplitudes
         d = self.dots[:k].cpu().numpy()
         B = np.zeros((k, k))
         B[:k - 1, :k - 1] = self.B
@@ -54,6 +51,7 @@ class DIIS:
         self.B = B
 
     def extrapolate(self, amps: torch.Tensor) -> torch.Tensor:
+        """New amplitudes sum_i c_i t_i, written into ``amps`` (which the history never aliases)."""
         if self.max_diis == 0:
             return amps
         if len(self.errors) > self.max_diis:
@@ -67,10 +65,9 @@ class DIIS:
         rhs = np.zeros(k + 1)
         rhs[-1] = -1.0
         c = np.linalg.solve(Bb, rhs)
-        out = torch.empty_like(amps)
         ptrs = (C.c_void_p * k)(*[x.data_ptr() for x in self.vals[1:]])
         coef = (C.c_double * k)(*[float(x) for x in c[:k]])
-        _lib.call("pcg_lincomb_f64", ptrs, coef, k, amps.numel(), out.data_ptr(),
+        _lib.call("pcg_lincomb_f64", ptrs, coef, k, amps.numel(), amps.data_ptr(),
                   _lib.stream_handle(self.stream))
-        self.old = out.clone()
-        return out
+        self.old = amps.clone()
+        return amps
