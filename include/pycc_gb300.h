@@ -72,6 +72,16 @@ int pcg_energy_f64(const double* fov, const long long* fs2, const double* L,
 int pcg_dots_f64(const double* x, const double* const* ys, int k, long long n, double* work,
                  long long work_len, double* out, void* stream);
 
+/* Allocation-free pcg_dots_f64 (no counterpart in the reference): out[j] = <x, ys[j]> for
+ * 1 <= k <= 8, with the partial sums kept in a fixed 64 KB array inside this library
+ * instead of a caller-provided work buffer.  For host programs that own all device memory
+ * (or must avoid cudaMalloc's implicit synchronisation) and so cannot hand the library
+ * scratch.  The first call on a device looks the array's device address up
+ * (cudaGetSymbolAddress); make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race.  k > 8 is rejected. */
+int pcg_dots_f64_noalloc(const double* x, const double* const* ys, int k, long long n,
+                         double* out, void* stream);
+
 /* e = x - old (e written; e must not alias x or old) and, in the same pass,
  * out[j] = <e, ys[j]> for j < k-1 and out[k-1] = <e, e>; 1 <= k <= 16 (ys: host array of
  * k-1 device pointers); work >= 1024*k doubles.  helper_diis.add_error_vector and the

@@ -32,6 +32,7 @@ SIGNATURES = {
     "pcg_update_amps_f64": (C.c_int, [_p, _p, _p, _p, _p, _i64, _i64, _p, _i64, _p, _p]),
     "pcg_energy_f64": (C.c_int, [_p, _pi64, _p, _pi64, _p, _p, _i64, _i64, _p, _i64, _p, _p]),
     "pcg_dots_f64": (C.c_int, [_p, C.POINTER(_p), C.c_int, _i64, _p, _i64, _p, _p]),
+    "pcg_dots_f64_noalloc": (C.c_int, [_p, C.POINTER(_p), C.c_int, _i64, _p, _p]),
     "pcg_lincomb_f64": (C.c_int, [C.POINTER(_p), C.POINTER(_d), C.c_int, _i64, _p, _p]),
     "pcg_diis_error_f64": (C.c_int, [_p, _p, _p, C.POINTER(_p), C.c_int, _i64, _p, _i64, _p, _p]),
     "pcg_pack_operand": (C.c_int, [C.c_int, C.c_int, _pi64, _pi64, C.c_int, _pi64, _pi64, _i64,

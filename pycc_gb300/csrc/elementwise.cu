@@ -360,3 +360,91 @@ extern "C" int pcg_diis_error_f64(const double* x, const double* old, double* e,
   PCG_CHECK_LAUNCH("pcg_diis_error_f64");
   return 0;
 }
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free variant of pcg_dots_f64.
+//
+// Some host programs cannot let a library allocate device memory: quantum-chemistry codes
+// that carve the whole GPU into their own arena up front (a library cudaMalloc then fails
+// or fragments it), and loops that must not pay cudaMalloc/cudaFree, which can synchronise
+// the device.  pcg_dots_f64 needs k*1024 doubles of scratch for its per-block partial
+// sums; this variant keeps that scratch in a fixed array of this library instead, so the
+// caller passes only the inputs and the output.
+//
+// * Limit: at most kNoAllocMaxVec (8) vectors per call, i.e. 8*1024 doubles (64 KB) of
+//   scratch, which every GPU that loads the library holds until the process exits.
+// * The array lives in device memory; host code only sees a stand-in symbol, so its device
+//   address is looked up once per device (cudaGetSymbolAddress) on the first call made
+//   with that device current.  Make that first call before any stream capture.
+// * Every call shares the array.  Each call writes every partial it later reads, so no
+//   clearing is needed, but calls that overlap on the GPU (different streams, or several
+//   host threads) race on it: serialise them.
+// ---------------------------------------------------------------------------------------
+#include <mutex>
+
+namespace pcg {
+namespace {
+constexpr int kNoAllocMaxVec = 8;
+static __device__ __align__(256) double g_dots_scratch[kNoAllocMaxVec * RED_BLOCKS];
+
+constexpr int kMaxDevices = 64;
+double* g_dots_scratch_ptr[kMaxDevices] = {nullptr};
+std::mutex g_dots_scratch_mu;
+
+// Device address of g_dots_scratch on the current device (looked up once per device).
+double* dots_scratch_address() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("pcg_dots_f64_noalloc: cudaGetDevice failed: %s", cudaGetErrorString(e));
+    return nullptr;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("pcg_dots_f64_noalloc: device ordinal %d out of range", dev);
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(g_dots_scratch_mu);
+  if (!g_dots_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_dots_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("pcg_dots_f64_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return nullptr;
+    }
+    g_dots_scratch_ptr[dev] = static_cast<double*>(p);
+  }
+  return g_dots_scratch_ptr[dev];
+}
+}  // namespace
+}  // namespace pcg
+
+// out[j] = <x, ys[j]> for 1 <= k <= 8, with no device allocation (see above).
+extern "C" int pcg_dots_f64_noalloc(const double* x, const double* const* ys, int k, long long n,
+                                    double* out, void* stream) {
+  if (k < 1 || k > kNoAllocMaxVec) {
+    set_error("pcg_dots_f64_noalloc: k=%d outside [1, %d] (the fixed scratch holds %d vectors; "
+              "use pcg_dots_f64 with a caller-provided work buffer for more)",
+              k, kNoAllocMaxVec, kNoAllocMaxVec);
+    return -1;
+  }
+  if (!x || !ys || !out || n < 0) {
+    set_error("pcg_dots_f64_noalloc: bad arguments");
+    return -1;
+  }
+  for (int j = 0; j < k; ++j)
+    if (!ys[j]) {
+      set_error("pcg_dots_f64_noalloc: ys[%d] is null", j);
+      return -1;
+    }
+  double* scratch = dots_scratch_address();
+  if (!scratch) return -3;
+  cudaStream_t st = (cudaStream_t)stream;
+  VecList v{};
+  for (int j = 0; j < k; ++j) v.p[j] = ys[j];
+  const int nb = std::min(ew_blocks(n), RED_BLOCKS);
+  dots_kernel<<<nb, EW_THREADS, 0, st>>>(x, v, k, n, scratch);
+  PCG_CHECK_LAUNCH("pcg_dots_f64_noalloc/partials");
+  finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(scratch, nb, k, out);
+  PCG_CHECK_LAUNCH("pcg_dots_f64_noalloc");
+  return 0;
+}
