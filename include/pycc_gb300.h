@@ -107,26 +107,29 @@ int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n
  *   row_scale[r] = 2^ceil(log2(max_k |v| / 448)); 3 three BF16 pieces hi = bf16(v),
  *   mid = bf16(v - hi), lo = bf16(v - hi - mid).  Rows are Kp elements long (zero padded);
  *   Kp is a multiple of 64 (BF16) or 128 (FP8).  X or P (with Q) must be given; Y may be
- *   NULL; mid is used by format 3 only. */
+ *   NULL; mid is used by format 3 only.  row_tab (optional, device, [4][rows]) gives the
+ *   four sources' row offsets explicitly (e.g. the i <= j pairs of a symmetric operand);
+ *   the r sub-indices are then ignored and `rows` rows are packed. */
 int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* r_str, int k_n,
                      const long long* k_ext, const long long* k_str, long long Kp, double a,
                      const double* X, double b, const double* Y, double c, const double* P,
                      const double* Q, void* hi, void* mid, void* lo, float* row_scale,
-                     void* stream);
+                     const long long* row_tab, long long rows, void* stream);
 
 /* pcg_tc_gemm: C[off_m(m) + off_n(n)] = beta*C + alpha * sum_k A[m][k] B[n][k] (C FP64).
  *   A: M rows of lda elements (K-major, 16-byte aligned rows), B: N rows of ldb elements;
  *   format as above: 1 = three tcgen05 passes Al.Bh + Ah.Bl + Ah.Bh, 3 = the six piece
  *   products of order <= 2^-16 (smallest first), 2 = FP8 with the row scales applied in the
  *   epilogue.  off_m / off_n: flat index over up to 4 sub-indices (extents, element strides
- *   in C).  status: device int, set non-zero when a bounded device-side wait expired (the
- *   kernel then skips its stores). */
+ *   in C); col_map (optional, device, N entries) replaces off_n and col_scale (optional,
+ *   device, N doubles) multiplies each column.  status: device int, set non-zero when a
+ *   bounded device-side wait expired (the kernel then skips its stores). */
 int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, long long M,
                 long long lda, const void* B_hi, const void* B_mid, const void* B_lo, long long N,
                 long long ldb, long long Kp, const float* a_scale, const float* b_scale, int m_n,
                 const long long* m_ext, const long long* m_sc, int n_n, const long long* n_ext,
-                const long long* n_sc, double alpha, double beta, double* C, int* status,
-                void* stream);
+                const long long* n_sc, const long long* col_map, const double* col_scale,
+                double alpha, double beta, double* C, int* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -36,10 +36,10 @@ SIGNATURES = {
     "pcg_lincomb_f64": (C.c_int, [C.POINTER(_p), C.POINTER(_d), C.c_int, _i64, _p, _p]),
     "pcg_diis_error_f64": (C.c_int, [_p, _p, _p, C.POINTER(_p), C.c_int, _i64, _p, _i64, _p, _p]),
     "pcg_pack_operand": (C.c_int, [C.c_int, C.c_int, _pi64, _pi64, C.c_int, _pi64, _pi64, _i64,
-                                   _d, _p, _d, _p, _d, _p, _p, _p, _p, _p, _p, _p]),
+                                   _d, _p, _d, _p, _d, _p, _p, _p, _p, _p, _p, _p, _i64, _p]),
     "pcg_tc_gemm": (C.c_int, [C.c_int, _p, _p, _p, _i64, _i64, _p, _p, _p, _i64, _i64, _i64,
-                              _p, _p, C.c_int, _pi64, _pi64, C.c_int, _pi64, _pi64, _d, _d, _p,
-                              _p, _p]),
+                              _p, _p, C.c_int, _pi64, _pi64, C.c_int, _pi64, _pi64, _p, _p, _d,
+                              _d, _p, _p, _p]),
 }
 
 _lib = None

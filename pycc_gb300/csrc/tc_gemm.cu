@@ -69,6 +69,8 @@ struct Args {
   double* C;
   const float* a_scale;
   const float* b_scale;
+  const long long* col_map;   // optional per-column C offsets (replaces en)
+  const double* col_scale;    // optional per-column multipliers
   int atomic_out;
   int* status;
 };
@@ -192,14 +194,21 @@ __device__ __forceinline__ long long epi_offset(const EpiIdx& d, long long r) {
   return o;
 }
 
+constexpr int kSmemMax = 232448;  // 227 KB of dynamic shared memory per CTA
+
 template <int BN>
 struct Smem {
   static constexpr int A_BYTES = BM * KBYTES;
   static constexpr int B_BYTES = BN * KBYTES;
   static constexpr int STAGE = A_BYTES + B_BYTES;
-  static constexpr int STAGES = (BN >= 256) ? 4 : (BN >= 128 ? 6 : 8);
-  static constexpr int TAIL = 512 + 4 * BN * 8;  // barriers, tmem slot, flags, column offsets
+  // barriers / tmem slot / flags, then per epilogue warp BN column offsets and scales
+  static constexpr int TAIL = 512 + 4 * BN * 16;
+  static constexpr int FIT = (kSmemMax - 1024 - TAIL) / STAGE;
+  static constexpr int STAGES = FIT > 8 ? 8 : FIT;
   static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
+  static constexpr unsigned TMEM_COLS = (2 * BN <= 128) ? 128 : ((2 * BN <= 256) ? 256 : 512);
+  static_assert(BN % 32 == 0 && BN >= 64 && BN <= 256, "BN: multiple of 32 in [64, 256]");
+  static_assert(STAGES >= 3, "shared-memory ring too shallow");
 };
 
 // Tile t -> (split, m tile, n tile); N tiles fastest so CTAs running together share A.
@@ -223,7 +232,7 @@ __global__ void __launch_bounds__(NT, 1)
     tc_gemm_kernel(const __grid_constant__ Maps maps, const Args p) {
   using L = Smem<BN>;
   constexpr int S = L::STAGES;
-  constexpr uint32_t TMEM_COLS = 2 * BN;
+  constexpr uint32_t TMEM_COLS = L::TMEM_COLS;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
@@ -238,6 +247,7 @@ __global__ void __launch_bounds__(NT, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   long long* colofs_all = reinterpret_cast<long long*>(tail + 512);  // [4 warps][BN]
+  double* colsc_all = reinterpret_cast<double*>(tail + 512 + 4 * BN * 8);  // [4 warps][BN]
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long ntiles = p.mt * p.nt * p.splits;
@@ -370,6 +380,7 @@ __global__ void __launch_bounds__(NT, 1)
     // ---- epilogue warps: TMEM -> registers -> FP64 C, one chunk at a time ----
     const int q = warp & 3;  // the TMEM lane quarter this warp may read
     long long* colofs = colofs_all + (warp - 2) * BN;  // this warp's copy
+    double* colsc = colsc_all + (warp - 2) * BN;
     int u = 0;
     bool stop = false;
     for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
@@ -386,7 +397,12 @@ __global__ void __launch_bounds__(NT, 1)
       __syncwarp();  // the previous tile's column offsets are no longer read
       for (int j = lane; j < BN; j += 32) {
         const long long c = n0 + j;
-        colofs[j] = (c < p.N) ? epi_offset(p.en, c) : -1;
+        const bool in = c < p.N;
+        colofs[j] = in ? (p.col_map ? p.col_map[c] : epi_offset(p.en, c)) : -1;
+        double sc = p.alpha;
+        if (in && p.fp8) sc *= (double)p.b_scale[c];
+        if (in && p.col_scale) sc *= p.col_scale[c];
+        colsc[j] = sc;
       }
       __syncwarp();
       bool first = true;
@@ -426,8 +442,7 @@ __global__ void __launch_bounds__(NT, 1)
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             if (co[j] < 0) continue;
-            double v = (double)__uint_as_float(r[j]) * p.alpha;
-            if (p.fp8) v *= ascale * (double)p.b_scale[n0 + cc + j];
+            const double v = (double)__uint_as_float(r[j]) * ascale * colsc[cc + j];
             if (p.atomic_out)
               atomicAdd(crow + co[j], v);
             else
@@ -484,6 +499,7 @@ struct PackArgs {
   void* lo;
   void* mid;
   float* scale;
+  const long long* row_tab;  // optional [4][R] per-source row offsets (replaces r)
   int fmt;
 };
 
@@ -514,7 +530,12 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile& t, l
   const int tid = threadIdx.x;
   if (tid < TR) {
     long long o[4] = {0, 0, 0, 0};
-    if (r0 + tid < p.R) pack_offsets(p.r, r0 + tid, o);
+    if (r0 + tid < p.R) {
+      if (p.row_tab)
+        for (int s = 0; s < 4; ++s) o[s] = p.row_tab[s * p.R + r0 + tid];
+      else
+        pack_offsets(p.r, r0 + tid, o);
+    }
     for (int s = 0; s < 4; ++s) t.rof[s][tid] = o[s];
   } else if (tid >= 64 && tid < 64 + TK) {
     const int j = tid - 64;
@@ -735,9 +756,11 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
                                 int k_n, const long long* k_ext, const long long* k_str,
                                 long long Kp, double a, const double* X, double b,
                                 const double* Y, double c, const double* P, const double* Q,
-                                void* hi, void* mid, void* lo, float* row_scale, void* stream) {
+                                void* hi, void* mid, void* lo, float* row_scale,
+                                const long long* row_tab, long long rows, void* stream) {
   PackArgs p{};
   if (!fill_pack(p.r, r_n, r_ext, r_str) || !fill_pack(p.k, k_n, k_ext, k_str)) return -1;
+  p.row_tab = row_tab;
   if (fmt < 0 || fmt > 3 || (!X && !P) || !hi || ((fmt == kBF16x3 || fmt == kBF16x6) && !lo) ||
       (fmt == kBF16x6 && !mid) || (fmt == kFP8 && !row_scale) || (P && !Q)) {
     set_error("pcg_pack_operand: bad pointers for format %d", fmt);
@@ -745,6 +768,13 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   }
   p.R = 1;
   for (int q = 0; q < p.r.n; ++q) p.R *= p.r.ext[q];
+  if (row_tab) {
+    if (rows <= 0) {
+      set_error("pcg_pack_operand: a row table needs rows > 0");
+      return -1;
+    }
+    p.R = rows;
+  }
   p.K = 1;
   for (int q = 0; q < p.k.n; ++q) p.K *= p.k.ext[q];
   const int kblk = (fmt == kFP8) ? 128 : 64;
@@ -799,7 +829,8 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
                            const void* B_lo, long long N, long long ldb, long long Kp,
                            const float* a_scale, const float* b_scale, int m_n,
                            const long long* m_ext, const long long* m_sc, int n_n,
-                           const long long* n_ext, const long long* n_sc, double alpha,
+                           const long long* n_ext, const long long* n_sc,
+                           const long long* col_map, const double* col_scale, double alpha,
                            double beta, double* C, int* status, void* stream) {
   if (fmt < 0 || fmt > 3) {
     set_error("pcg_tc_gemm: unknown format %d", fmt);
@@ -844,8 +875,21 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.C = C;
   a.a_scale = a_scale;
   a.b_scale = b_scale;
+  a.col_map = col_map;
+  a.col_scale = col_scale;
   a.status = status;
-  const int BN = (N <= 64) ? 64 : (N <= 128 ? 128 : 256);
+  // tile width: least padded work, weighting each tile by its fixed A-operand share
+  static const int kBN[] = {64, 96, 128, 160, 192, 224, 256};
+  int BN = 64;
+  long long best = -1;
+  for (int bn : kBN) {
+    const long long tiles_n = (N + bn - 1) / bn;
+    const long long cost = tiles_n * (bn + 48);
+    if (best < 0 || cost < best || (cost == best && bn > BN)) {
+      best = cost;
+      BN = bn;
+    }
+  }
   long long mt = (M + BM - 1) / BM, nt = (N + BN - 1) / BN;
   if (mt > 0x7fffffffLL || nt > 0x7fffffffLL) {
     set_error("pcg_tc_gemm: too many tiles (M tiles %lld)", mt);
@@ -884,7 +928,11 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   }
   switch (BN) {
     case 64: return launch<64>(maps, a, st);
+    case 96: return launch<96>(maps, a, st);
     case 128: return launch<128>(maps, a, st);
+    case 160: return launch<160>(maps, a, st);
+    case 192: return launch<192>(maps, a, st);
+    case 224: return launch<224>(maps, a, st);
     default: return launch<256>(maps, a, st);
   }
 }

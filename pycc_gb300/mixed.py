@@ -17,11 +17,12 @@ one-body matrices before they multiply t2.
 """
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from . import _lib
 from .contract import contract_f64
-from .tc import FMT_BF16, FMT_BF16X3, FMT_BF16X6, FMT_FP8, Operand, TCEngine
+from .tc import FMT_BF16, FMT_BF16X3, FMT_BF16X6, FMT_FP8, Operand, TCEngine, pack
 
 
 class MixedResidual:
@@ -50,6 +51,7 @@ class MixedResidual:
         self.bad = 0
         self.history = []
         self.profile = None       # list of (subscripts, fmt, start, end) events when set
+        self._pairs = None        # i <= j pair tables of the ladder
 
     # -- precision schedule ---------------------------------------------------------------
     def select_mode(self, rms):
@@ -120,6 +122,39 @@ class MixedResidual:
     @staticmethod
     def t2op(labels, t2, t2lab=None):
         return Operand.of(labels, t2) if t2lab is None else Operand(labels, (t2, t2lab))
+
+    # -- the <ab|ef> ladder over i <= j pairs (pycc/ccwfn.py:931) ---------------------------
+    def _pair_tables(self):
+        if self._pairs is None:
+            no, nv = self.w.no, self.w.nv
+            ii, jj = np.triu_indices(no)
+            tab = np.zeros((4, ii.size), dtype=np.int64)
+            tab[0] = ii * no * nv * nv + jj * nv * nv       # t2[i, j, :, :]
+            tab[2] = ii * nv                                # t1[i, :]
+            tab[3] = jj * nv                                # t1[j, :]
+            cmap = (ii * no * nv * nv + jj * nv * nv).astype(np.int64)
+            csc = np.where(ii == jj, 0.5, 1.0)
+            dev = self.w.device1
+            self._pairs = (torch.from_numpy(tab).to(dev), torch.from_numpy(cmap).to(dev),
+                           torch.from_numpy(csc).to(dev))
+        return self._pairs
+
+    def ladder_pairs(self, t1, t2, r, fmt):
+        """r_ijab += 1/2 tau_ijef <ab|ef> through the i <= j pairs only.
+
+        tau_jife = tau_ijef and <ba|fe> = <ab|ef>, so the term is symmetric under
+        (i<->j, a<->b) and the symmetrisation r2 = h + h' of r_T2 (ccwfn.py:790) doubles it.
+        Writing the full term for i < j into h (and half of it for i = j) and nothing for
+        i > j gives the same symmetrised residual with o(o+1)/2 instead of o^2 rows.
+        """
+        if not r.is_contiguous():
+            raise ValueError("ladder_pairs: the half residual must be contiguous")
+        tab, cmap, csc = self._pair_tables()
+        tau = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
+        pb = pack(tau, ['i', 'j'], ['e', 'f'], fmt, self.w.stream, row_tab=tab)
+        pa = self.tc._pack(self.eri('vvvv', 'abef'), ['a', 'b'], ['e', 'f'], fmt, 'A')
+        self.tc.run_gemm('ijef,abef->ijab', fmt, pa, pb, r, ['a', 'b'], [], 'ijab', 1.0, 1.0,
+                         col_map=cmap, col_scale=csc)
 
     # -- intermediates (pycc/ccwfn.py:458-715) -------------------------------------------
     def build_Fae(self, F, t1, t2):
@@ -210,9 +245,7 @@ class MixedResidual:
         # ladders
         tau_mn = Operand('mnab', (t2, 'mnab'), P=(t1, 'ma'), Q=(t1, 'nb'), c=1.0)
         self.tcc('mnab,mnij->ijab', tau_mn, Operand.of('mnij', Wmnij), r, alpha=0.5)
-        tau_ij = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
-        self.tcc('ijef,abef->ijab', tau_ij, self.eri('vvvv', 'abef'), r, alpha=0.5,
-                 fmt=self.ladder_fmt())
+        self.ladder_pairs(t1, t2, r, self.ladder_fmt())
         self.tcc('ma,mbij->ijab', Operand.of('ma', t1), Operand.of('mbij', Zmbij), r, alpha=-1.0)
         # rings
         self.tcc('imae,mbej->ijab', Operand('imae', (t2, 'imae'), Y=(t2, 'imea'), b=-1.0),

@@ -103,11 +103,13 @@ def kblock(fmt):
     return 128 if fmt == FMT_FP8 else 64
 
 
-def pack(op: Operand, row_labels, k_labels, fmt, stream=None) -> Packed:
+def pack(op: Operand, row_labels, k_labels, fmt, stream=None, row_tab=None) -> Packed:
+    """Pack ``op`` with rows over ``row_labels`` (or the explicit per-source row offsets
+    ``row_tab``, an int64 [4, R] device tensor) and K over ``k_labels``."""
     ext = op.extents()
     rows = [(ext[c], op.strides(c)) for c in row_labels]
     ks = [(ext[c], op.strides(c)) for c in k_labels]
-    R = math.prod(ext[c] for c in row_labels)
+    R = math.prod(ext[c] for c in row_labels) if row_tab is None else int(row_tab.shape[1])
     K = math.prod(ext[c] for c in k_labels)
     rows, ks = _merge_multi(rows), _merge_multi(ks)
     if len(rows) > MAX_SUB or len(ks) > MAX_SUB:
@@ -140,19 +142,22 @@ def pack(op: Operand, row_labels, k_labels, fmt, stream=None) -> Packed:
               float(op.a), _ptr(op.X), float(op.b), _ptr(op.Y), float(op.c), _ptr(op.P),
               _ptr(op.Q), hi.data_ptr(), mid.data_ptr() if mid is not None else None,
               lo.data_ptr() if lo is not None else None,
-              scale.data_ptr() if scale is not None else None, _lib.stream_handle(stream))
+              scale.data_ptr() if scale is not None else None,
+              row_tab.data_ptr() if row_tab is not None else None,
+              R if row_tab is not None else 0, _lib.stream_handle(stream))
     return Packed(fmt, R, Kp, hi, lo, scale, mid)
 
 
 def gemm(fmt, A: Packed, B: Packed, out, row_labels, col_labels, out_labels, alpha=1.0,
-         beta=1.0, status=None, stream=None):
-    """out = beta*out + alpha * A . B^T with rows/cols mapped to ``out`` through labels."""
+         beta=1.0, status=None, stream=None, col_map=None, col_scale=None):
+    """out = beta*out + alpha * A . B^T with rows/cols mapped to ``out`` through labels
+    (or, for the columns, the explicit offsets ``col_map`` and multipliers ``col_scale``)."""
     if A.Kp != B.Kp:
         raise ValueError("gemm: K mismatch %d vs %d" % (A.Kp, B.Kp))
     ost = dict(zip(out_labels, out.stride()))
     oext = dict(zip(out_labels, out.shape))
     mg = _merge_multi([(oext[c], [ost[c]]) for c in row_labels])
-    ng = _merge_multi([(oext[c], [ost[c]]) for c in col_labels])
+    ng = _merge_multi([(oext[c], [ost[c]]) for c in col_labels]) if col_map is None else []
     if len(mg) > MAX_SUB or len(ng) > MAX_SUB:
         raise ValueError("gemm: more than %d output sub-indices" % MAX_SUB)
     i64 = _lib.i64s
@@ -164,6 +169,8 @@ def gemm(fmt, A: Packed, B: Packed, out, row_labels, col_labels, out_labels, alp
               B.scale.data_ptr() if B.scale is not None else None,
               len(mg), i64([g[0] for g in mg]), i64([g[1][0] for g in mg]),
               len(ng), i64([g[0] for g in ng]), i64([g[1][0] for g in ng]),
+              col_map.data_ptr() if col_map is not None else None,
+              col_scale.data_ptr() if col_scale is not None else None,
               float(alpha), float(beta), out.data_ptr(), status.data_ptr(),
               _lib.stream_handle(stream))
 
@@ -214,18 +221,23 @@ class TCEngine:
             A, B, ma, nb = B, A, nb, ma
         pa = self._pack(A, ma, kk, fmt, "A")
         pb = self._pack(B, nb, kk, fmt, "B")
+        self.run_gemm(subscripts, fmt, pa, pb, out, ma, nb, rhs, alpha, beta)
+        return out
+
+    def run_gemm(self, subscripts, fmt, pa, pb, out, rows, cols, rhs, alpha, beta,
+                 col_map=None, col_scale=None):
+        """One tensor-core GEMM launch, timed with CUDA events when ``self.timing`` is set."""
         ev = None
         if self.timing is not None:
             st = torch.cuda.current_stream() if self.stream is None else self.stream
             ev = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             ev[0].record(st)
-        gemm(fmt, pa, pb, out, ma, nb, rhs, alpha=alpha, beta=beta, status=self.status,
-             stream=self.stream)
+        gemm(fmt, pa, pb, out, rows, cols, rhs, alpha=alpha, beta=beta, status=self.status,
+             stream=self.stream, col_map=col_map, col_scale=col_scale)
         if ev is not None:
             ev[1].record(st)
             self.timing.append({"subs": subscripts, "fmt": fmt, "M": pa.rows, "N": pb.rows,
                                 "Kp": pa.Kp, "start": ev[0], "end": ev[1]})
-        return out
 
     def _pack(self, op, rows, ks, fmt, side):
         if op.key is None:

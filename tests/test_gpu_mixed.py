@@ -22,7 +22,8 @@ def frob(a, b):
 
 
 @pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_FP8])
-@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (200, 70, 100), (37, 300, 513)])
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (200, 70, 100), (37, 300, 513), (64, 180, 96),
+                                   (100, 210, 64), (150, 150, 64), (300, 820, 200)])
 def test_gemm_exact_integers(cuda, fmt, M, N, K):
     g = torch.Generator(device=cuda).manual_seed(M + N + K)
     A = torch.randint(-3, 4, (M, K), generator=g, device=cuda).double()
