@@ -40,6 +40,19 @@ int pcg_contract_f64(int m_n, const long long* m_ext, const long long* m_sa,
                      double alpha, const double* A, const double* B, double beta, double* C,
                      void* stream);
 
+/* Sum of up to four FP64 contractions into one output (written once):
+ *   C = beta*C + sum_t alpha[t] * A_t[m,k] B_t[n,k]
+ * Common M / N extents and C strides (m_ext, m_sc, n_ext, n_sc); per term t the A strides
+ * of the M sub-indices m_sa[t*4+q], the B strides of the N sub-indices n_sb[t*4+q] and its
+ * own K group (k_n[t]; k_ext, k_sa, k_sb at [t*4+q]); A, B, alpha: host arrays of nterm.
+ * The four t3 terms of one output orientation, t3c_ijk (pycc/cctriples.py:56-67). */
+int pcg_contract_multi_f64(int nterm, int m_n, const long long* m_ext, const long long* m_sc,
+                           const long long* m_sa, int n_n, const long long* n_ext,
+                           const long long* n_sc, const long long* n_sb, const int* k_n,
+                           const long long* k_ext, const long long* k_sa, const long long* k_sb,
+                           const double* alpha, const double* const* A, const double* const* B,
+                           double beta, double* C, void* stream);
+
 /* ---- FP64 elementwise kernels ---------------------------------------------------------- */
 /* tau_ijab = f1*t2_ijab + f2*t1_ia*t1_jb; CCwfn.build_tau (pycc/ccwfn.py:432-455) */
 int pcg_tau_f64(const double* t1, const double* t2, long long no, long long nv, double f1,
@@ -95,6 +108,22 @@ int pcg_diis_error_f64(const double* x, const double* old, double* e, const doub
 int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n, double* out,
                     void* stream);
 
+/* ---- (T) ---------------------------------------------------------------------------
+ * Lee-Rendell E(T) of the reference's t_tjl (pycc/cctriples.py:177-240) for ntrip triples
+ * ijk[t] = (i, j, k), i >= j >= k.  The connected triples of triple t are given as three
+ * partial tensors (v^3 each, pstride elements apart between triples):
+ *   W[a,b,c] = P1[a][b][c] + P2[a][c][b] + P3[b][c][a]
+ * the disconnected triples (t3d_ijk, :108-147) are formed from eoovv = <ij|ab>, t1 and, if
+ * fov is not NULL, t2 and f_ov.  fp32 != 0: FP32 partials and element arithmetic, else
+ * FP64.  Writes part[t*nv + a] (FP64, weight (2 - d_ij - d_ik - d_jk) applied). */
+int pcg_triples_energy(int fp32, const void* P1, const void* P2, const void* P3,
+                       long long pstride, const int* ijk, int ntrip, const double* eps,
+                       const double* eoovv, const double* t1, const double* t2,
+                       const double* fov, long long no, long long nv, double* part,
+                       void* stream);
+/* *out += sum(x[0:n]) in FP64 (one block, deterministic). */
+int pcg_reduce_sum_f64(const double* x, long long n, double* out, void* stream);
+
 /* ---- tensor-core (tcgen05) contraction engine, mixed-precision path ------------------
  * The GB300 replacement of the low-precision path of the same contractions (pycc/ccwfn.py:
  * 458-945 through pycc/device.py:64-87); the reference's own low-precision mode is plain
@@ -130,6 +159,20 @@ int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, 
                 const long long* m_ext, const long long* m_sc, int n_n, const long long* n_ext,
                 const long long* n_sc, const long long* col_map, const double* col_scale,
                 double alpha, double beta, double* C, int* status, void* stream);
+
+/* Grouped segmented BF16 GEMM with FP32 output, the connected-triples builder of the (T)
+ * correction (t3c_ijk, pycc/cctriples.py:56-67, for a batch of triples).  Group g computes
+ *   C[out_g + m*ldc + n] = sum_s A[amap_gs][arow_gs + m, :] . B[bmap_gs][brow_gs + n, :]
+ * for m < M, n < N over its nseg <= 4 K segments (nkb_gs K blocks of 64).  a_ptr / b_ptr:
+ * host arrays of up to four BF16 K-major operand matrices (a_rows[q] rows of a_ld[q]
+ * elements).  groups: device array of ngroups records of pcg_tc_group_desc_size() bytes:
+ *   int nseg; int amap[4], arow[4], bmap[4], brow[4], nkb[4]; (pad) long long out. */
+int pcg_tc_grouped_gemm(int na, const void* const* a_ptr, const long long* a_rows,
+                        const long long* a_ld, int nb, const void* const* b_ptr,
+                        const long long* b_rows, const long long* b_ld, const void* groups,
+                        int ngroups, long long M, long long N, float* C, long long ldc,
+                        int* status, void* stream);
+int pcg_tc_group_desc_size(void);
 
 #ifdef __cplusplus
 }

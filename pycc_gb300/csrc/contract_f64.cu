@@ -358,3 +358,201 @@ extern "C" int pcg_contract_f64(int m_n, const long long* m_ext, const long long
   PCG_CHECK_LAUNCH("pcg_contract_f64");
   return 0;
 }
+
+// ---------------------------------------------------------------------------------------
+// Sum of up to four FP64 contractions into one output tile:
+//   C[m, n] = beta * C[m, n] + sum_t alpha_t * sum_k A_t[m, k] * B_t[n, k]
+// All terms share the M / N extents and the C strides; each term has its own operands, A / B
+// strides and K range.  Used where several einsum terms land on the same output (the four
+// terms of one orientation of the connected triples), so the output is written once.
+// ---------------------------------------------------------------------------------------
+namespace pcg {
+namespace {
+constexpr int kMaxTerms = 4;
+
+struct MultiArgs {
+  int nterm;
+  SubIdx m, n;                 // ext + C strides (s1); s0 unused
+  long long ma[kMaxTerms][kMaxSub];  // per-term A strides of the M sub-indices
+  long long nb[kMaxTerms][kMaxSub];  // per-term B strides of the N sub-indices
+  SubIdx k[kMaxTerms];         // per-term K (A strides s0, B strides s1)
+  long long K[kMaxTerms];
+  double alpha[kMaxTerms];
+  const double* A[kMaxTerms];
+  const double* B[kMaxTerms];
+  long long M, N;
+  double beta;
+  double* C;
+};
+
+__device__ __forceinline__ long long strided_offset(const SubIdx& d, const long long* s,
+                                                    long long r) {
+  long long o = 0;
+  for (int q = d.n - 1; q >= 0; --q) {
+    const long long e = d.ext[q];
+    o += (r % e) * s[q];
+    r /= e;
+  }
+  return o;
+}
+
+__global__ void __launch_bounds__(NT) contract_multi_f64_kernel(const MultiArgs p) {
+  __shared__ double As[BK][BM + 2];
+  __shared__ double Bs[BK][BN + 2];
+  __shared__ long long aoff[BM], coffm[BM], boff[BN], coffn[BN];
+  __shared__ long long akoff[BK], bkoff[BK];
+  const int tid = threadIdx.x;
+  const long long m0 = (long long)blockIdx.y * BM;
+  const long long n0 = (long long)blockIdx.x * BN;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int wm = warp >> 1, wn = warp & 1;
+  const int g = lane >> 2, t4 = lane & 3;
+  double acc[4][4][2];
+  if (tid < BM) {
+    const long long r = m0 + tid;
+    coffm[tid] = (r < p.M) ? strided_offset(p.m, p.m.s1, r) : 0;
+  } else {
+    const int t = tid - BM;
+    const long long r = n0 + t;
+    coffn[t] = (r < p.N) ? strided_offset(p.n, p.n.s1, r) : 0;
+  }
+  double out[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) out[i][j][0] = out[i][j][1] = 0.0;
+
+  for (int term = 0; term < p.nterm; ++term) {
+    __syncthreads();
+    if (tid < BM) {
+      const long long r = m0 + tid;
+      aoff[tid] = (r < p.M) ? strided_offset(p.m, p.ma[term], r) : 0;
+    } else {
+      const int t = tid - BM;
+      const long long r = n0 + t;
+      boff[t] = (r < p.N) ? strided_offset(p.n, p.nb[term], r) : 0;
+    }
+    const SubIdx& kd = p.k[term];
+    const long long K = p.K[term];
+    const double* Ap = p.A[term];
+    const double* Bp = p.B[term];
+    const int a_kfast = (kd.s0[kd.n - 1] == 1);
+    const int b_kfast = (kd.s1[kd.n - 1] == 1);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+    for (long long kt = 0; kt < K; kt += BK) {
+      __syncthreads();
+      if (tid < BK) {
+        long long o0 = 0, o1 = 0;
+        if (kt + tid < K) sub_offsets(kd, kt + tid, o0, o1);
+        akoff[tid] = o0;
+        bkoff[tid] = o1;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int e = tid + NT * i;
+        int mm, kk;
+        if (a_kfast) { kk = e % BK; mm = e / BK; } else { mm = e % BM; kk = e / BM; }
+        As[kk][mm] = (m0 + mm < p.M && kt + kk < K) ? __ldg(Ap + aoff[mm] + akoff[kk]) : 0.0;
+        int nn;
+        if (b_kfast) { kk = e % BK; nn = e / BK; } else { nn = e % BN; kk = e / BN; }
+        Bs[kk][nn] = (n0 + nn < p.N && kt + kk < K) ? __ldg(Bp + boff[nn] + bkoff[kk]) : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int ks = 0; ks < BK; ks += 4) {
+        double a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[ks + t4][wm * 32 + i * 8 + g];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[ks + t4][wn * 32 + j * 8 + g];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) dmma(acc[i][j], a[i], b[j]);
+      }
+    }
+    const double al = p.alpha[term];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        out[i][j][0] += al * acc[i][j][0];
+        out[i][j][1] += al * acc[i][j][1];
+      }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int row = wm * 32 + i * 8 + g;
+    if (m0 + row >= p.M) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int col = wn * 32 + j * 8 + 2 * t4 + h;
+        if (n0 + col >= p.N) continue;
+        double* dst = p.C + coffm[row] + coffn[col];
+        *dst = (p.beta == 0.0) ? out[i][j][h] : p.beta * *dst + out[i][j][h];
+      }
+  }
+}
+}  // namespace
+}  // namespace pcg
+
+// C = beta*C + sum_t alpha[t] * A_t . B_t^T over nterm (<= 4) terms.  The M / N sub-index
+// extents (m_ext, n_ext) and C strides (m_sc, n_sc) are common; per term t: A strides of the
+// M sub-indices m_sa[t*4 + q], B strides of the N sub-indices n_sb[t*4 + q], and its K
+// group k_n[t], k_ext[t*4 + q], k_sa[t*4 + q], k_sb[t*4 + q].
+extern "C" int pcg_contract_multi_f64(int nterm, int m_n, const long long* m_ext,
+                                      const long long* m_sc, const long long* m_sa, int n_n,
+                                      const long long* n_ext, const long long* n_sc,
+                                      const long long* n_sb, const int* k_n,
+                                      const long long* k_ext, const long long* k_sa,
+                                      const long long* k_sb, const double* alpha,
+                                      const double* const* A, const double* const* B,
+                                      double beta, double* C, void* stream) {
+  using namespace pcg;
+  if (nterm < 1 || nterm > kMaxTerms || m_n < 0 || m_n > kMaxSub || n_n < 0 || n_n > kMaxSub ||
+      !C) {
+    set_error("pcg_contract_multi_f64: bad term / sub-index counts");
+    return -1;
+  }
+  MultiArgs p{};
+  p.nterm = nterm;
+  const long long zero[kMaxSub] = {0, 0, 0, 0};
+  if (!fill_sub(p.m, m_n, m_ext, zero, m_sc, "M") || !fill_sub(p.n, n_n, n_ext, zero, n_sc, "N"))
+    return -1;
+  for (int t = 0; t < nterm; ++t) {
+    for (int q = 0; q < kMaxSub; ++q) {
+      p.ma[t][q] = (q < m_n) ? m_sa[t * kMaxSub + q] : 0;
+      p.nb[t][q] = (q < n_n) ? n_sb[t * kMaxSub + q] : 0;
+    }
+    if (!fill_sub(p.k[t], k_n[t], k_ext + t * kMaxSub, k_sa + t * kMaxSub, k_sb + t * kMaxSub,
+                  "K"))
+      return -1;
+    p.K[t] = sub_total(p.k[t]);
+    p.alpha[t] = alpha[t];
+    p.A[t] = A[t];
+    p.B[t] = B[t];
+    if (!A[t] || !B[t]) {
+      set_error("pcg_contract_multi_f64: null operand of term %d", t);
+      return -1;
+    }
+  }
+  p.M = sub_total(p.m);
+  p.N = sub_total(p.n);
+  p.beta = beta;
+  p.C = C;
+  const long long mt = (p.M + BM - 1) / BM, nt = (p.N + BN - 1) / BN;
+  if (mt > 65535) {
+    set_error("pcg_contract_multi_f64: M=%lld too large", p.M);
+    return -1;
+  }
+  dim3 grid((unsigned)nt, (unsigned)mt);
+  contract_multi_f64_kernel<<<grid, NT, 0, (cudaStream_t)stream>>>(p);
+  PCG_CHECK_LAUNCH("pcg_contract_multi_f64");
+  return 0;
+}

@@ -1,0 +1,101 @@
+"""(T) correction on the GPU against the reference's energies and the CPU oracle.
+
+Tolerances: FP64 path 1e-11 Eh (absolute) against t_tjl / t_vikings; the BF16 tensor-core
+path within 2e-3 relative of the FP64 value; the grouped GEMM is exact on integer data.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+import pycc_gb300 as pg
+from pycc_gb300 import _lib
+from pycc_gb300.triples import t_energy_fp64
+from pycc_gb300.triples_tc import GROUP_DTYPE, t_energy_tc
+from pycc_gb300.tc import FMT_BF16, Operand, pack
+from oracle import ccsd as oc
+from oracle import triples as ot
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def w1(cuda, cfg1_ham, cfg1):
+    _, F, ERI, L = cfg1_ham
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda))
+    w.t1.copy_(torch.from_numpy(cfg1["t1"]))
+    w.t2.copy_(torch.from_numpy(np.ascontiguousarray(cfg1["t2"])))
+    return w
+
+
+def test_fp64_triples_cfg1(w1, cfg1):
+    et = t_energy_fp64(w1)
+    assert abs(et - float(cfg1["et_tjl"])) < 1e-11
+    assert abs(et - float(cfg1["et_vikings"])) < 1e-11
+
+
+def test_tc_triples_cfg1(w1, cfg1):
+    et = t_energy_tc(w1, batch=7)
+    ref = float(cfg1["et_tjl"])
+    assert abs(et - ref) < 2e-3 * abs(ref), (et, ref)
+
+
+@pytest.mark.parametrize("no,nv", [(3, 17), (6, 23)])
+def test_triples_vs_oracle(cuda, no, nv):
+    fac = pg.SyntheticFactors(no, nv, seed=11, coupling="matched")
+    F, ERI, L = fac.hamiltonian()
+    t1, t2 = oc.mp2_guess(F, ERI, no)
+    rng = np.random.default_rng(no + nv)
+    t1 = 0.01 * rng.standard_normal((no, nv))
+    ref = ot.t_tjl(no, nv, F, ERI, t1, t2)
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, no, L=L, device=cuda))
+    w.t1.copy_(torch.from_numpy(t1))
+    et = t_energy_fp64(w)
+    assert abs(et - ref) < 1e-11 * max(1.0, abs(ref) * 1e3)
+    et_tc = t_energy_tc(w, batch=5)
+    assert abs(et_tc - ref) < 2e-3 * abs(ref)
+
+
+def test_ccsd_t_model(cuda, cfg1_ham, cfg1):
+    _, F, ERI, L = cfg1_ham
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda), model="CCSD(T)")
+    e = w.solve_cc(1e-12, 1e-12, 100)
+    assert abs(e - (float(cfg1["ecc"]) + float(cfg1["et_tjl"]))) < 1e-10
+
+
+def test_grouped_gemm_exact(cuda):
+    """Two groups with two K segments each, integer data: exact against torch."""
+    g = torch.Generator(device=cuda).manual_seed(3)
+    M, N = 300, 150
+    A0 = torch.randint(-3, 4, (2 * M, 64), generator=g, device=cuda).double()
+    A1 = torch.randint(-3, 4, (M, 128), generator=g, device=cuda).double()
+    B0 = torch.randint(-3, 4, (N + 20, 64), generator=g, device=cuda).double()
+    B1 = torch.randint(-3, 4, (2 * N, 128), generator=g, device=cuda).double()
+    pk = lambda X: pack(Operand.of("rk", X), ["r"], ["k"], FMT_BF16)
+    pa, pb = [pk(A0), pk(A1)], [pk(B0), pk(B1)]
+    gd = np.zeros(2, dtype=GROUP_DTYPE)
+    # group 0: A0[0:M] B0[0:N] + A1 B1[N:2N];  group 1: A0[M:2M] B0[20:20+N]
+    gd[0]["nseg"] = 2
+    gd[0]["amap"][:2], gd[0]["arow"][:2] = [0, 1], [0, 0]
+    gd[0]["bmap"][:2], gd[0]["brow"][:2], gd[0]["nkb"][:2] = [0, 1], [0, N], [1, 2]
+    gd[0]["out"] = 0
+    gd[1]["nseg"] = 1
+    gd[1]["amap"][0], gd[1]["arow"][0], gd[1]["bmap"][0], gd[1]["brow"][0] = 0, M, 0, 20
+    gd[1]["nkb"][0] = 1
+    gd[1]["out"] = M * N
+    gt = torch.from_numpy(gd.view(np.uint8)).to(cuda)
+    out = torch.full((2, M, N), float("nan"), dtype=torch.float32, device=cuda)
+    st = torch.zeros(4, dtype=torch.int32, device=cuda)
+    a_ptr = (C.c_void_p * 2)(*[x.hi.data_ptr() for x in pa])
+    b_ptr = (C.c_void_p * 2)(*[x.hi.data_ptr() for x in pb])
+    _lib.call("pcg_tc_grouped_gemm", 2, a_ptr, _lib.i64s([x.rows for x in pa]),
+              _lib.i64s([x.Kp for x in pa]), 2, b_ptr, _lib.i64s([x.rows for x in pb]),
+              _lib.i64s([x.Kp for x in pb]), gt.data_ptr(), 2, M, N, out.data_ptr(), N,
+              st.data_ptr(), _lib.stream_handle())
+    torch.cuda.synchronize()
+    ref0 = A0[:M] @ B0[:N].T + A1 @ B1[N:].T
+    ref1 = A0[M:] @ B0[20:20 + N].T
+    assert torch.equal(out[0].double(), ref0)
+    assert torch.equal(out[1].double(), ref1)
+    assert int(st.abs().sum()) == 0
