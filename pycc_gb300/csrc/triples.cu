@@ -42,19 +42,24 @@ __device__ __forceinline__ T wval(const TripArgs<T>& p, const T* P1, const T* P2
   return P1[(x * v + y) * v + z] + P2[(x * v + z) * v + y] + P3[(y * v + z) * v + x];
 }
 
-// disconnected triples (pycc/cctriples.py:133-140) at (x, y, z)
+// disconnected triples (pycc/cctriples.py:133-140) at (x, y, z), in the arithmetic type T
+// (FP32 for the tensor-core path: the FP64 pipe of GB300 is ~60x slower than FP32)
 template <typename T>
 __device__ __forceinline__ T dval(const TripArgs<T>& p, int i, int j, int k, long long x,
                                   long long y, long long z) {
   const long long o = p.no, v = p.nv;
-  auto E = [&](int a, int b, long long c, long long d) { return p.eoovv[((a * o + b) * v + c) * v + d]; };
-  auto A2 = [&](int a, int b, long long c, long long d) { return p.t2[((a * o + b) * v + c) * v + d]; };
-  double d = E(i, j, x, y) * p.t1[k * v + z] + E(i, k, x, z) * p.t1[j * v + y] +
-             E(j, k, y, z) * p.t1[i * v + x];
+  auto E = [&](int a, int b, long long c, long long d) {
+    return (T)p.eoovv[((a * o + b) * v + c) * v + d];
+  };
+  auto A2 = [&](int a, int b, long long c, long long d) {
+    return (T)p.t2[((a * o + b) * v + c) * v + d];
+  };
+  T d = E(i, j, x, y) * (T)p.t1[k * v + z] + E(i, k, x, z) * (T)p.t1[j * v + y] +
+        E(j, k, y, z) * (T)p.t1[i * v + x];
   if (p.fov)
-    d += A2(i, j, x, y) * p.fov[k * v + z] + A2(i, k, x, z) * p.fov[j * v + y] +
-         A2(j, k, y, z) * p.fov[i * v + x];
-  return (T)d;
+    d += A2(i, j, x, y) * (T)p.fov[k * v + z] + A2(i, k, x, z) * (T)p.fov[j * v + y] +
+         A2(j, k, y, z) * (T)p.fov[i * v + x];
+  return d;
 }
 
 template <typename T>
@@ -69,7 +74,7 @@ __global__ void __launch_bounds__(TE_THREADS) triples_energy_kernel(const TripAr
   const double eo = p.eps[i] + p.eps[j] + p.eps[k];
   const double fac = 2.0 - ((i == j) + (i == k) + (j == k));
   const long long npair = (a + 1) * (a + 2) / 2;
-  double acc = 0.0;
+  T acc_t = 0;  // per-thread partial (a few hundred terms); the block sum is FP64
   for (long long q = threadIdx.x; q < npair; q += TE_THREADS) {
     // q -> (b, c) with a >= b >= c
     long long b = (long long)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
@@ -93,9 +98,10 @@ __global__ void __launch_bounds__(TE_THREADS) triples_energy_kernel(const TripAr
     const T Wc = W[0] + W[3] + W[4];
     const T Wa = W[1] + W[2] + W[5];
     const T S = (Y - (T)2 * Z) * Wc + (Z - (T)2 * Y) * Wa + (T)3 * X;
-    const double D = eo - p.eps[o + a] - p.eps[o + b] - p.eps[o + c];
-    acc += (double)S / D;
+    const T D = (T)(eo - p.eps[o + a] - p.eps[o + b] - p.eps[o + c]);
+    acc_t += S / D;
   }
+  double acc = (double)acc_t;
   __shared__ double red[TE_THREADS / 32];
   for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
