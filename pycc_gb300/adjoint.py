@@ -1,0 +1,321 @@
+"""Adjoint of the converged CCSD energy: Lambda equations and gradient densities.
+
+The FP64 residual (``CCwfn.residuals``) and the energy are recorded on a tape as the
+engine's own operations (strided contractions, copies, combinations, tau builds, the r2
+symmetrisation).  Reverse accumulation through that tape, with the same CUDA kernels,
+gives the vector-Jacobian products of the residual:
+
+* J^T lambda (with respect to the amplitudes): one Lambda iteration.  The Lambda equations
+  ``J^T lambda = -dE/dt`` replace the reference's hand-derived ``cclambda``
+  (``pycc/cclambda.py:69-560``); they are solved by the same Jacobi + DIIS iteration as
+  the amplitudes (``lambda += (dE/dt + J^T lambda) / D``).
+* dE/dH at the converged (t, lambda): with respect to the Fock matrix and every
+  integral block read by the residual.  Assembled into the full ``D`` (nmo x nmo) and
+  ``Gamma`` (nmo^4, <pq|rs> order) they are the gradient densities of the reference's
+  ``ccdensity.gradient_densities`` (``pycc/ccdensity.py:267-333``): E_corr = <D,F> + <Gamma,ERI>.
+  The reference stores representative blocks and symmetrises them 4-fold; both agree on the
+  8-fold permutationally symmetric projection, the part any symmetric perturbation sees.
+
+vvvv-sized cotangents are never stored separately: the ladder's adjoint contractions write
+straight into the gradient buffers of tau and of the <ab|ef> block.
+"""
+from __future__ import annotations
+
+import math
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .contract import contract_f64
+from .diis import DIIS
+from .exceptions import ConvergenceError
+from .hamiltonian import ERI_BLOCKS, L_BLOCKS, _sl
+
+WORK_LEN = 4096
+
+
+class Tape:
+    def __init__(self):
+        self.ops = []
+
+    def record(self, kind, *args):
+        self.ops.append((kind, args))
+
+
+def _base(t):
+    return t._base if t._base is not None else t
+
+
+def _key(t):
+    return _base(t).untyped_storage().data_ptr()
+
+
+class Grads:
+    """Gradient buffers keyed by storage; views of a tensor map to views of its buffer."""
+
+    def __init__(self):
+        self.buf = {}
+
+    def clear(self):
+        self.buf = {}
+
+    def get(self, t, create=True):
+        b = _base(t)
+        k = _key(t)
+        g = self.buf.get(k)
+        if g is None:
+            if not create:
+                return None
+            g = torch.zeros(b.shape, dtype=torch.float64, device=b.device)
+            self.buf[k] = g
+        return g.as_strided(t.size(), t.stride(), t.storage_offset() - b.storage_offset())
+
+    def has(self, t):
+        return _key(t) in self.buf
+
+
+def _as4(t):
+    while t.dim() < 4:
+        t = t.unsqueeze(0)
+    return t
+
+
+def accumulate(dst, src, a=1.0, perm=None, stream=None):
+    """dst += a * src (src optionally read through ``perm``); in place, FP64 kernel."""
+    d4 = _as4(dst)
+    s = src.permute(*perm) if perm is not None else src
+    s4 = _as4(s)
+    _lib.call("pcg_combine4_f64", _lib.i64s(d4.shape), 1.0, d4.data_ptr(), _lib.i64s(d4.stride()),
+              float(a), s4.data_ptr(), _lib.i64s(s4.stride()), d4.data_ptr(),
+              _lib.i64s(d4.stride()), _lib.stream_handle(stream))
+
+
+def _inverse(perm):
+    inv = [0] * len(perm)
+    for i, p in enumerate(perm):
+        inv[p] = i
+    return tuple(inv)
+
+
+class CCSDAdjoint:
+    """Tape of the FP64 residual + energy at the amplitudes of a converged ``CCwfn``."""
+
+    def __init__(self, w):
+        if w.precision != 'DP':
+            raise ValueError("the adjoint runs on the FP64 path (precision='DP')")
+        self.w = w
+        self.stream = w.stream
+        H = w.H
+        self.leaves_H = set()
+        for t in [H.F] + list(H.ERI.blocks.values()) + list(H.L.blocks.values()):
+            self.leaves_H.add(_key(t))
+        self.t1, self.t2 = w.t1, w.t2
+        tape = Tape()
+        w._tape = tape
+        try:
+            self.r1, self.r2 = w.residuals(H.F, self.t1, self.t2)
+            self.E = w.cc_energy_contractions(w.o, w.v, H.F, H.L, self.t1, self.t2)
+        finally:
+            w._tape = None
+        self.tape = tape
+        self.grads = Grads()
+        self.wrt_H = False
+        self._work = torch.empty(WORK_LEN, dtype=torch.float64, device=H.F.device)
+        self._scal = torch.zeros(4, dtype=torch.float64, device=H.F.device)
+
+    # -- reverse accumulation -------------------------------------------------------------
+    def _want(self, t):
+        return self.wrt_H or _key(t) not in self.leaves_H
+
+    def backward(self, gE=0.0, l1=None, l2=None, wrt_H=False, seed=None):
+        """Accumulate cotangents (gE on E, l1 on r1, l2 on r2) back to the leaves.
+
+        ``seed`` maps leaf tensors to initial gradient values (added before the sweep).
+        """
+        self.wrt_H = wrt_H
+        G = self.grads
+        G.clear()
+        st = self.stream
+        if seed:
+            for t, val in seed.items():
+                accumulate(G.get(t), val, stream=st)
+        if gE != 0.0:
+            gEt = G.get(self.E)
+            gEt.fill_(float(gE))
+        if l1 is not None:
+            accumulate(G.get(self.r1), l1, stream=st)
+        if l2 is not None:
+            accumulate(G.get(self.r2), l2, stream=st)
+        for kind, args in reversed(self.tape.ops):
+            getattr(self, "_bw_" + kind)(*args)
+        return G
+
+    def _bw_contract(self, subs, A, B, out, alpha, beta):
+        G = self.grads
+        if not G.has(out):
+            return
+        gZ = G.get(out)
+        lhs, rhs = subs.replace(" ", "").split("->")
+        la, lb = lhs.split(",")
+        if self._want(A):
+            contract_f64("%s,%s->%s" % (rhs, lb, la), gZ, B, out=G.get(A), alpha=alpha, beta=1.0,
+                         stream=self.stream)
+        if self._want(B):
+            contract_f64("%s,%s->%s" % (la, rhs, lb), A, gZ, out=G.get(B), alpha=alpha, beta=1.0,
+                         stream=self.stream)
+
+    def _bw_copy(self, X, out):
+        G = self.grads
+        if G.has(out) and self._want(X):
+            accumulate(G.get(X), G.get(out), stream=self.stream)
+
+    def _bw_combine(self, a, X, b, Y, perm, out):
+        G = self.grads
+        if not G.has(out):
+            return
+        gO = G.get(out)
+        if a != 0.0 and self._want(X):
+            accumulate(G.get(X), gO, a, stream=self.stream)
+        if Y is not None and b != 0.0 and self._want(Y):
+            accumulate(G.get(Y), gO, b, perm=_inverse(perm), stream=self.stream)
+
+    def _bw_tau(self, t1, t2, f1, f2, out):
+        G = self.grads
+        if not G.has(out):
+            return
+        gO = G.get(out)
+        if f1 != 0.0:
+            accumulate(G.get(t2), gO, f1, stream=self.stream)
+        if f2 != 0.0:
+            g1 = G.get(t1)
+            contract_f64("ijab,jb->ia", gO, t1, out=g1, alpha=f2, beta=1.0, stream=self.stream)
+            contract_f64("ijab,ia->jb", gO, t1, out=g1, alpha=f2, beta=1.0, stream=self.stream)
+
+    def _bw_sym(self, h, out):
+        G = self.grads
+        if not G.has(out):
+            return
+        gO = G.get(out)
+        gh = G.get(h)
+        accumulate(gh, gO, stream=self.stream)
+        accumulate(gh, gO, perm=(1, 0, 3, 2), stream=self.stream)
+
+    # -- Lambda equations -----------------------------------------------------------------
+    def dE_dt(self):
+        G = self.backward(gE=1.0)
+        return G.get(self.t1).clone(), G.get(self.t2).clone()
+
+    def jt_lambda(self, l1, l2, g1, g2):
+        """(dE/dt1 + J^T l)_1, (...)_2: the Lambda residual."""
+        G = self.backward(l1=l1, l2=l2, seed={self.t1: g1, self.t2: g2})
+        return G.get(self.t1), G.get(self.t2)
+
+    def solve_lambda(self, e_conv=1e-10, r_conv=1e-10, maxiter=100, max_diis=8, start_diis=1,
+                     callback=None):
+        """Jacobi + DIIS on J^T lambda = -dE/dt; returns (l1, l2)."""
+        w = self.w
+        no, nv = w.no, w.nv
+        t0 = time.time()
+        g1, g2 = self.dE_dt()
+        lam = torch.zeros(no * nv + no * no * nv * nv, dtype=torch.float64, device=g1.device)
+        l1 = lam[:no * nv].view(no, nv)
+        l2 = lam[no * nv:].view(no, no, nv, nv)
+        diis = DIIS(lam, max_diis, self.stream)
+        self.lambda_times = []
+        pseudo_last, rms = 0.0, float("inf")
+        for niter in range(1, maxiter + 1):
+            ti = time.time()
+            R1, R2 = self.jt_lambda(l1, l2, g1, g2)
+            out = self._scal[1:2]
+            _lib.call("pcg_update_amps_f64", l1.data_ptr(), l2.data_ptr(), R1.data_ptr(),
+                      R2.data_ptr(), w.H.eps.data_ptr(), no, nv, self._work.data_ptr(),
+                      self._work.numel(), out.data_ptr(), _lib.stream_handle(self.stream))
+            # pseudo-energy: <lambda, dE/dt> (stationary at convergence)
+            pe = contract_f64("ia,ia->", l1, g1, stream=self.stream)
+            contract_f64("ijab,ijab->", l2, g2, out=pe, beta=1.0, stream=self.stream)
+            vals = torch.stack([out.reshape(()), pe.reshape(())]).cpu().numpy()
+            rms, pseudo = math.sqrt(max(float(vals[0]), 0.0)), float(vals[1])
+            self.lambda_times.append(time.time() - ti)
+            if callback is not None:
+                callback(niter, pseudo, pseudo - pseudo_last, rms)
+            if abs(pseudo - pseudo_last) < e_conv and rms < r_conv:
+                self.l1, self.l2 = l1, l2
+                self.lambda_niter = niter
+                self.timing_lambda = time.time() - t0
+                return l1, l2
+            pseudo_last = pseudo
+            diis.add_error_vector(lam)
+            if niter >= start_diis:
+                diis.extrapolate(lam)
+        raise ConvergenceError("Lambda", maxiter, pseudo - pseudo_last, rms)
+
+    # -- gradient densities ---------------------------------------------------------------
+    def gradient(self, e_conv=1e-10, r_conv=1e-10, maxiter=100):
+        """dE/dF (nmo x nmo) and dE/d<pq|rs> (nmo^4) at the converged amplitudes."""
+        if not hasattr(self, "l1"):
+            self.solve_lambda(e_conv, r_conv, maxiter)
+        t0 = time.time()
+        G = self.backward(gE=1.0, l1=self.l1, l2=self.l2, wrt_H=True)
+        w = self.w
+        H = w.H
+        no, nv, n = w.no, w.nv, w.nmo
+        gF = G.get(H.F).clone()
+        Gam = torch.zeros((n, n, n, n), dtype=torch.float64, device=gF.device)
+        for pat, blk in H.ERI.blocks.items():
+            if G.has(blk):
+                s = _sl(pat, no, nv)
+                accumulate(Gam[s[0], s[1], s[2], s[3]], G.get(blk), stream=self.stream)
+        for pat, blk in H.L.blocks.items():
+            if G.has(blk):
+                s = _sl(pat, no, nv)
+                g = G.get(blk)
+                accumulate(Gam[s[0], s[1], s[2], s[3]], g, 2.0, stream=self.stream)
+                accumulate(Gam[s[0], s[1], s[3], s[2]], g, -1.0, perm=(0, 1, 3, 2),
+                           stream=self.stream)
+        torch.cuda.synchronize()
+        self.timing_gradient = time.time() - t0
+        self.grads.clear()
+        return gF, Gam
+
+
+def symmetrize8(G):
+    """Projection of a <pq|rs> tensor onto the 8-fold permutational symmetry of real ERIs."""
+    # <pq|rs> = (pr|qs); the chemist tensor is symmetric under p<->r, q<->s and (pr)<->(qs)
+    C = G.permute(0, 2, 1, 3)
+    C = 0.5 * (C + C.permute(1, 0, 2, 3))
+    C = 0.5 * (C + C.permute(0, 1, 3, 2))
+    C = 0.5 * (C + C.permute(2, 3, 0, 1))
+    return C.permute(0, 2, 1, 3).contiguous()
+
+
+class CCSDEnergy(torch.autograd.Function):
+    """Converged FP64 CCSD correlation energy of (F, <pq|rs>) with its implicit adjoint.
+
+    forward: ``CCwfn.solve_cc`` on the GPU.  backward: the Lambda equations through the
+    residual's tape, then dE/dF and dE/d<pq|rs> (the gradient densities).
+    """
+
+    @staticmethod
+    def forward(ctx, F, ERI, no, e_conv=1e-11, r_conv=1e-11):
+        from .ccwfn import CCwfn
+        from .hamiltonian import Hamiltonian
+        H = Hamiltonian.from_full(F.detach(), ERI.detach(), int(no))
+        w = CCwfn(H, precision='DP')
+        e = w.solve_cc(e_conv, r_conv, 200)
+        ctx.w = w
+        ctx.conv = (e_conv, r_conv)
+        return torch.tensor(e, dtype=torch.float64, device=F.device)
+
+    @staticmethod
+    def backward(ctx, gE):
+        adj = CCSDAdjoint(ctx.w)
+        adj.solve_lambda(*ctx.conv)
+        gF, Gam = adj.gradient()
+        return gE * gF, gE * Gam, None, None, None
+
+
+def ccsd_energy(F, ERI, no, e_conv=1e-11, r_conv=1e-11):
+    """Differentiable FP64 CCSD correlation energy (see :class:`CCSDEnergy`)."""
+    return CCSDEnergy.apply(F, ERI, no, e_conv, r_conv)

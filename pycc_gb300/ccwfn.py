@@ -102,7 +102,9 @@ class CCwfn:
         self.v = slice(self.no, self.nmo)
         self.device1 = H.device
         self.stream = None
-        self.contract = ContractionBackend(self.device1, self.stream)
+        self._backend = ContractionBackend(self.device1, self.stream)
+        self._tape = None         # set by pycc_gb300.adjoint while a residual is recorded
+        self.contract = self._contract
         self._work = torch.empty(WORK_LEN, dtype=torch.float64, device=self.device1)
         self._scalars = torch.zeros(8, dtype=torch.float64, device=self.device1)
 
@@ -143,18 +145,43 @@ class CCwfn:
     def _st(self):
         return _lib.stream_handle(self.stream)
 
+    def _contract(self, subscripts, *operands, out=None, alpha=1.0, beta=0.0):
+        """``self.contract`` (pycc/device.py:64-87) on the FP64 engine; recorded on the
+        adjoint tape when one is active."""
+        fresh = out is None
+        res = self._backend(subscripts, *operands, out=out, alpha=alpha, beta=beta)
+        if self._tape is not None:
+            self._tape.record("contract", subscripts, operands[0], operands[1], res, alpha,
+                              0.0 if fresh else beta)
+        return res
+
+    def _copy(self, X):
+        """Contiguous copy of a (possibly strided) 2- or 4-index tensor (FP64 kernel)."""
+        if X.dim() == 2:
+            X4 = X.reshape(1, 1, *X.shape) if X.is_contiguous() else X.unsqueeze(0).unsqueeze(0)
+            out = torch.empty(X.shape, dtype=torch.float64, device=X.device)
+            self._combine(1.0, X4, 0.0, None, None, out=out.view(1, 1, *X.shape), record=False)
+        else:
+            out = self._combine(1.0, X, 0.0, None, None, record=False)
+        if self._tape is not None:
+            self._tape.record("copy", X, out)
+        return out
+
     # -- pycc/ccwfn.py:432-455 ------------------------------------------------------------
     def build_tau(self, t1, t2, fact1=1.0, fact2=1.0):
         """tau_ijab = fact1 t2_ijab + fact2 t_ia t_jb (fused FP64 kernel)."""
-        t1 = t1.contiguous()
-        t2 = t2.contiguous()
+        if not (t1.is_contiguous() and t2.is_contiguous()):
+            raise ValueError("build_tau: t1 and t2 must be contiguous")
         out = torch.empty_like(t2)
         _lib.call("pcg_tau_f64", _ptr(t1), _ptr(t2), self.no, self.nv, float(fact1), float(fact2),
                   _ptr(out), self._st())
+        if self._tape is not None:
+            self._tape.record("tau", t1, t2, float(fact1), float(fact2), out)
         return out
 
-    def _combine(self, a, X, b, Y, perm_y, out=None):
+    def _combine(self, a, X, b, Y, perm_y, out=None, record=True):
         """out_pqrs = a X_pqrs + b Y_perm (4-index; perm_y permutes Y's axes)."""
+        fresh = out is None
         ext = list(X.shape)
         if out is None:
             out = torch.empty(ext, dtype=torch.float64, device=X.device)
@@ -165,12 +192,16 @@ class CCwfn:
         _lib.call("pcg_combine4_f64", _lib.i64s(ext), float(a), _ptr(X), _lib.i64s(X.stride()),
                   float(b), _ptr(Y) if Y is not None else None, _lib.i64s(ys), _ptr(out),
                   _lib.i64s(out.stride()), self._st())
+        if record and self._tape is not None:
+            if not fresh:
+                raise ValueError("_combine: only fresh outputs can be recorded")
+            self._tape.record("combine", float(a), X, float(b), Y, perm_y, out)
         return out
 
     # -- pycc/ccwfn.py:458-498 ------------------------------------------------------------
     def build_Fae(self, o, v, F, L, t1, t2):
         c = self.contract
-        Fae = F[v, v].clone()
+        Fae = self._copy(F[v, v])
         c('me,ma->ae', F[o, v], t1, out=Fae, alpha=-0.5, beta=1.0)
         c('mf,mafe->ae', t1, L[o, v, v, v], out=Fae, beta=1.0)
         c('mnaf,mnef->ae', self.build_tau(t1, t2, 1.0, 0.5), L[o, o, v, v], out=Fae, alpha=-1.0,
@@ -180,7 +211,7 @@ class CCwfn:
     # -- pycc/ccwfn.py:501-534 ------------------------------------------------------------
     def build_Fmi(self, o, v, F, L, t1, t2):
         c = self.contract
-        Fmi = F[o, o].clone()
+        Fmi = self._copy(F[o, o])
         c('ie,me->mi', t1, F[o, v], out=Fmi, alpha=0.5, beta=1.0)
         c('ne,mnie->mi', t1, L[o, o, o, v], out=Fmi, beta=1.0)
         c('inef,mnef->mi', self.build_tau(t1, t2, 1.0, 0.5), L[o, o, v, v], out=Fmi, beta=1.0)
@@ -188,14 +219,14 @@ class CCwfn:
 
     # -- pycc/ccwfn.py:537-565 ------------------------------------------------------------
     def build_Fme(self, o, v, F, L, t1):
-        Fme = F[o, v].clone()
+        Fme = self._copy(F[o, v])
         self.contract('nf,mnef->me', t1, L[o, o, v, v], out=Fme, beta=1.0)
         return Fme
 
     # -- pycc/ccwfn.py:568-604 ------------------------------------------------------------
     def build_Wmnij(self, o, v, ERI, t1, t2):
         c = self.contract
-        W = ERI[o, o, o, o].clone()
+        W = self._copy(ERI[o, o, o, o])
         c('je,mnie->mnij', t1, ERI[o, o, o, v], out=W, beta=1.0)
         c('ie,mnej->mnij', t1, ERI[o, o, v, o], out=W, beta=1.0)
         c('ijef,mnef->mnij', self.build_tau(t1, t2), ERI[o, o, v, v], out=W, beta=1.0)
@@ -204,7 +235,7 @@ class CCwfn:
     # -- pycc/ccwfn.py:607-646 ------------------------------------------------------------
     def build_Wmbej(self, o, v, ERI, L, t1, t2):
         c = self.contract
-        W = ERI[o, v, v, o].clone()
+        W = self._copy(ERI[o, v, v, o])
         c('jf,mbef->mbej', t1, ERI[o, v, v, v], out=W, beta=1.0)
         c('nb,mnej->mbej', t1, ERI[o, o, v, o], out=W, alpha=-1.0, beta=1.0)
         c('jnfb,mnef->mbej', self.build_tau(t1, t2, 0.5, 1.0), ERI[o, o, v, v], out=W, alpha=-1.0,
@@ -228,7 +259,7 @@ class CCwfn:
     # -- pycc/ccwfn.py:718-761 ------------------------------------------------------------
     def r_T1(self, o, v, F, ERI, L, t1, t2, Fae, Fme, Fmi):
         c = self.contract
-        r = F[v, o].transpose(0, 1).contiguous()
+        r = self._copy(F[v, o].transpose(0, 1))
         c('ie,ae->ia', t1, Fae, out=r, beta=1.0)
         c('mi,ma->ia', Fmi, t1, out=r, alpha=-1.0, beta=1.0)
         t2s = self._combine(2.0, t2, -1.0, t2, (0, 1, 3, 2))
@@ -243,6 +274,8 @@ class CCwfn:
         r = self._r_T2_half(o, v, F, ERI, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij)
         out = torch.empty_like(r)
         _lib.call("pcg_symmetrize_f64", _ptr(r), self.no, self.nv, _ptr(out), self._st())
+        if self._tape is not None:
+            self._tape.record("sym", r, out)
         return out
 
     def _r_T2_half(self, o, v, F, ERI, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij):
@@ -252,10 +285,10 @@ class CCwfn:
         c = self.contract
         no, nv = self.no, self.nv
         r = self._combine(0.5, ERI[v, v, o, o].permute(2, 3, 0, 1), 0.0, None, None)
-        Fbe = Fae.clone()
+        Fbe = self._copy(Fae)
         c('mb,me->be', t1, Fme, out=Fbe, alpha=-0.5, beta=1.0)
         c('ijae,be->ijab', t2, Fbe, out=r, beta=1.0)
-        Fmj = Fmi.clone()
+        Fmj = self._copy(Fmi)
         c('je,me->mj', t1, Fme, out=Fmj, alpha=0.5, beta=1.0)
         c('imab,mj->ijab', t2, Fmj, out=r, alpha=-1.0, beta=1.0)
         tau = self.build_tau(t1, t2)
@@ -301,6 +334,12 @@ class CCwfn:
         return self._mixed
 
     # -- pycc/ccwfn.py:1122-1162 ----------------------------------------------------------
+    def cc_energy_contractions(self, o, v, F, L, t1, t2):
+        """The energy as two contractions (the form the adjoint tape records)."""
+        E = self.contract('ia,ia->', F[o, v], t1, alpha=2.0)
+        self.contract('ijab,ijab->', self.build_tau(t1, t2), L[o, o, v, v], out=E, beta=1.0)
+        return E
+
     def cc_energy(self, o, v, F, L, t1, t2, out=None):
         """E = 2 f_ia t_ia + tau_ijab L_ijab as a 0-d FP64 GPU tensor (fused kernel)."""
         t1 = t1.contiguous()

@@ -95,6 +95,23 @@ class Hamiltonian:
         return cls(Ft, BlockTensor("ERI", no, nv, eri), BlockTensor("L", no, nv, ll), no, nv, device)
 
     @classmethod
+    def from_full(cls, F, ERI, no):
+        """Blocks of a full GPU-resident <pq|rs> (torch, FP64); L formed from it."""
+        device = ERI.device
+        n = F.shape[0]
+        nv = n - no
+        eri, ll = {}, {}
+        for pat in ERI_BLOCKS:
+            s = _sl(pat, no, nv)
+            eri[pat] = ERI[s[0], s[1], s[2], s[3]].contiguous()
+        for pat in L_BLOCKS:
+            s = _sl(pat, no, nv)
+            ll[pat] = (2.0 * ERI[s[0], s[1], s[2], s[3]]
+                       - ERI[s[0], s[1], s[3], s[2]].transpose(2, 3)).contiguous()
+        return cls(F.contiguous().clone(), BlockTensor("ERI", no, nv, eri),
+                   BlockTensor("L", no, nv, ll), no, nv, device)
+
+    @classmethod
     def from_factors(cls, fac, device="cuda:0", eri_blocks=ERI_BLOCKS, l_blocks=L_BLOCKS):
         """Build the blocks on the GPU from a :class:`pycc_gb300.synth.SyntheticFactors`."""
         device = torch.device(device)
