@@ -212,6 +212,14 @@ class CCSDAdjoint:
         G = self.backward(l1=l1, l2=l2, seed={self.t1: g1, self.t2: g2})
         return G.get(self.t1), G.get(self.t2)
 
+    def _sym_half(self, X):
+        """(X_ijab + X_jiba) / 2 into a new buffer (FP64 kernel)."""
+        out = torch.empty_like(X)
+        _lib.call("pcg_combine4_f64", _lib.i64s(X.shape), 0.5, X.data_ptr(), _lib.i64s(X.stride()),
+                  0.5, X.data_ptr(), _lib.i64s(X.permute(1, 0, 3, 2).stride()), out.data_ptr(),
+                  _lib.i64s(out.stride()), _lib.stream_handle(self.stream))
+        return out
+
     def solve_lambda(self, e_conv=1e-10, r_conv=1e-10, maxiter=100, max_diis=8, start_diis=1,
                      callback=None):
         """Jacobi + DIIS on J^T lambda = -dE/dt; returns (l1, l2)."""
@@ -228,6 +236,9 @@ class CCSDAdjoint:
         for niter in range(1, maxiter + 1):
             ti = time.time()
             R1, R2 = self.jt_lambda(l1, l2, g1, g2)
+            # t2 is constrained to t2_ijab = t2_jiba and r2 is symmetric, so the Lambda
+            # equations live on the symmetric subspace: project the t2 part of the residual
+            R2 = self._sym_half(R2)
             out = self._scal[1:2]
             _lib.call("pcg_update_amps_f64", l1.data_ptr(), l2.data_ptr(), R1.data_ptr(),
                       R2.data_ptr(), w.H.eps.data_ptr(), no, nv, self._work.data_ptr(),
