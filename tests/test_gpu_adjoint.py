@@ -83,7 +83,7 @@ def test_autograd_function(adj1, cfg1_ham, cuda):
     Ft = torch.from_numpy(F).to(cuda).requires_grad_(True)
     Et = torch.from_numpy(ERI).to(cuda).requires_grad_(True)
     E = ccsd_energy(Ft, Et, 5, 1e-12, 1e-12)
-    assert abs(float(E) - e) < 1e-10
+    assert abs(float(E.detach()) - e) < 1e-10
     E.backward()
     assert (Ft.grad - gF).abs().max().item() < 1e-9
     assert (Et.grad - Gam).abs().max().item() < 1e-9
@@ -94,8 +94,8 @@ def test_lambda_vjp_transpose(adj1, cuda):
     _, _, _, adj = adj1
     w = adj.w
     g = torch.Generator(device=cuda).manual_seed(1)
-    x1 = torch.randn(w.no, w.nv, dtype=torch.float64, device=cuda, generator=g) * 1e-4
-    x2 = torch.randn(w.no, w.no, w.nv, w.nv, dtype=torch.float64, device=cuda, generator=g) * 1e-4
+    x1 = torch.randn(w.no, w.nv, dtype=torch.float64, device=cuda, generator=g) * 1e-5
+    x2 = torch.randn(w.no, w.no, w.nv, w.nv, dtype=torch.float64, device=cuda, generator=g) * 1e-5
     l1 = torch.randn(w.no, w.nv, dtype=torch.float64, device=cuda, generator=g)
     l2 = torch.randn(w.no, w.no, w.nv, w.nv, dtype=torch.float64, device=cuda, generator=g)
     # J x by central differences of the residual (exact to O(eps^2) for the quartic map)
@@ -105,4 +105,4 @@ def test_lambda_vjp_transpose(adj1, cuda):
     lhs = float(((rp[0] - rm[0]) * l1).sum() + ((rp[1] - rm[1]) * l2).sum()) / 2.0
     G = adj.backward(l1=l1, l2=l2)
     rhs = float((G.get(adj.t1) * x1).sum() + (G.get(adj.t2) * x2).sum())
-    assert abs(lhs - rhs) < 1e-8 * max(abs(lhs), 1e-12) + 1e-14
+    assert abs(lhs - rhs) < 1e-7 * max(abs(lhs), 1e-12) + 1e-15
