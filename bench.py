@@ -163,6 +163,104 @@ def reference_arm(args, rank):
     print(json.dumps(line))
 
 
+def triples_mode(args, dev):
+    """(T) at no=30, nv=240 (seed 4, matched coupling): mixed CCSD, then the tensor-core (T);
+    errors against the FP64 energies of tests/golden/fp64_reference.json."""
+    import numpy as np
+    import torch
+    import pycc_gb300 as pg
+    from pycc_gb300.triples_tc import t_energy_tc
+    no, nv, seed = 30, 240, 4
+    fac = pg.SyntheticFactors(no, nv, seed, coupling="matched")
+    H = pg.Hamiltonian.from_factors(fac, device=dev)
+    w = pg.CCwfn(H, precision="MIXED")
+    t0 = time.time()
+    ecc = w.solve_cc(1e-8, 1e-7, 60)
+    torch.cuda.synchronize()
+    t_cc = time.time() - t0
+    t_energy_tc(w, batch=32)                    # warm-up (packs, kernels)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    et = t_energy_tc(w, batch=32)
+    e1.record()
+    torch.cuda.synchronize()
+    s = e0.elapsed_time(e1) / 1e3
+    flop = 2 * no**3 * nv**4 + 2 * no**4 * nv**3
+    ref = json.load(open(FP64_REF)).get("%d_%d_%d" % (no, nv, seed), {})
+    line = {"mode": "triples", "config": {"no": no, "nv": nv, "seed": seed, "coupling": "matched"},
+            "ccsd_mixed": {"ecc": ecc, "niter": w.niter, "s": t_cc,
+                           "ms_per_iter": 1e3 * float(np.mean(w.iter_times[1:]))},
+            "t_s": s, "t_tflops": flop / s / 1e12, "t_flop": flop, "et": et,
+            "et_fp64": ref.get("et"), "ecc_fp64": ref.get("ecc"),
+            "et_err": (et - ref["et"]) if "et" in ref else None,
+            "ecc_err": (ecc - ref["ecc"]) if "ecc" in ref else None,
+            "t_fp64_s": ref.get("t_s")}
+    print(json.dumps(line))
+
+
+def adjoint_mode(args, dev, directions=16):
+    """Adjoint at no=20, nv=180 (seed 3, matched coupling): Lambda + gradient densities,
+    backward/forward cost, central finite differences along random symmetric directions."""
+    import numpy as np
+    import torch
+    import pycc_gb300 as pg
+    from pycc_gb300.adjoint import CCSDAdjoint
+    from pycc_gb300.contract import contract_f64
+    no, nv, seed = 20, 180, 3
+    fac = pg.SyntheticFactors(no, nv, seed, coupling="matched")
+    H = pg.Hamiltonian.from_factors(fac, device=dev)
+    w = pg.CCwfn(H)
+    e = w.solve_cc(1e-12, 1e-12, 100)
+    fwd = float(np.mean(w.iter_times[1:]))
+    torch.cuda.synchronize()
+    t0 = time.time()
+    adj = CCSDAdjoint(w)
+    adj.solve_lambda(1e-12, 1e-12, 200)
+    gF, Gam = adj.gradient()
+    torch.cuda.synchronize()
+    t_back = time.time() - t0
+    n = no + nv
+    B = torch.from_numpy(fac.B).to(dev)
+    ERI = contract_f64("Qpr,Qqs->pqrs", B, B)
+    F = H.F
+    ident = float((gF * F).sum() + (Gam * ERI).sum()) - e
+    h, rows = 1e-5, []
+    for d in range(directions):
+        g = torch.Generator(device=dev).manual_seed(100 + d)
+        dF = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
+        dF = 0.5 * (dF + dF.T)
+        C = torch.randn(n, n, n, n, dtype=torch.float64, device=dev, generator=g)
+        C = 0.5 * (C + C.permute(1, 0, 2, 3))
+        C = 0.5 * (C + C.permute(0, 1, 3, 2))
+        C = 0.5 * (C + C.permute(2, 3, 0, 1))
+        dE = C.permute(0, 2, 1, 3).contiguous()
+        del C
+        nrm = float(torch.sqrt((dF * dF).sum() + (dE * dE).sum()))
+        dF /= nrm
+        dE /= nrm
+        an = float((gF * dF).sum() + (Gam * dE).sum())
+        es = []
+        for sg in (1.0, -1.0):
+            wp = pg.CCwfn(pg.Hamiltonian.from_full(F + sg * h * dF, ERI + sg * h * dE, no))
+            es.append(wp.solve_cc(1e-12, 1e-12, 200))
+            del wp
+        fd = (es[0] - es[1]) / (2 * h)
+        rows.append({"fd": fd, "adjoint": an, "abs": abs(fd - an), "rel": abs(fd - an) / abs(an)})
+        del dE, dF
+        torch.cuda.empty_cache()
+    line = {"mode": "adjoint", "config": {"no": no, "nv": nv, "seed": seed, "coupling": "matched"},
+            "ecc": e, "forward_iter_s": fwd, "forward_niter": w.niter,
+            "lambda_niter": adj.lambda_niter,
+            "lambda_iter_s": float(np.mean(adj.lambda_times[1:])),
+            "vjp_over_forward_iter": float(np.mean(adj.lambda_times[1:])) / fwd,
+            "backward_s": t_back, "backward_over_forward_iter": t_back / fwd,
+            "gradient_s": adj.timing_gradient, "energy_identity_err": ident,
+            "fd_max_abs": max(r["abs"] for r in rows), "fd_max_rel": max(r["rel"] for r in rows),
+            "fd": rows}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -180,10 +278,19 @@ def main():
                     help="start in the final precision stage (profiling of that stage)")
     ap.add_argument("--converge-iters", type=int, default=60,
                     help="untimed iterations allowed after the timed ones to reach the floor")
+    ap.add_argument("--mode", default="ccsd", choices=["ccsd", "triples", "adjoint"],
+                    help="ccsd: the benchmark line; triples / adjoint: the (T) and adjoint "
+                         "measurements at no=30,nv=240 and no=20,nv=180")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, rank)
+        return
+    if args.mode != "ccsd":
+        import torch
+        dev = torch.device("cuda:%d" % local)
+        torch.cuda.set_device(dev)
+        (triples_mode if args.mode == "triples" else adjoint_mode)(args, dev)
         return
 
     import numpy as np
