@@ -73,6 +73,15 @@ int pcg_update_amps_f64(double* t1, double* t2, const double* r1, const double* 
                         const double* eps, long long no, long long nv, double* work,
                         long long work_len, double* rms2, void* stream);
 
+/* inv1[i,a] = 1/(e_i - e_a), inv2[i,j,a,b] = 1/(e_i + e_j - e_a - e_b) from eps[nmo];
+ * the denominators of pycc/ccwfn.py:195-198, computed once per Hamiltonian. */
+int pcg_inv_denominators_f64(const double* eps, long long no, long long nv, double* inv1,
+                             double* inv2, void* stream);
+/* t += r * inv over n elements; *rms2 = sum (r*inv)^2 (device scalar); work >= 1024 doubles.
+ * The same update as pcg_update_amps_f64 with the divides replaced by products. */
+int pcg_update_inv_f64(double* t, const double* r, const double* inv, long long n, double* work,
+                       long long work_len, double* rms2, void* stream);
+
 /* *out = 2 sum f_ia t_ia + sum (t2_ijab + t_ia t_jb) L_ijab (device scalar); f: o x v with
  * strides fs[2], L: oovv with strides ls[4]; work >= 1024 doubles.
  * CCwfn.cc_energy (pycc/ccwfn.py:1122-1162) */

@@ -30,6 +30,8 @@ SIGNATURES = {
     "pcg_combine4_f64": (C.c_int, [_pi64, _d, _p, _pi64, _d, _p, _pi64, _p, _pi64, _p]),
     "pcg_symmetrize_f64": (C.c_int, [_p, _i64, _i64, _p, _p]),
     "pcg_update_amps_f64": (C.c_int, [_p, _p, _p, _p, _p, _i64, _i64, _p, _i64, _p, _p]),
+    "pcg_inv_denominators_f64": (C.c_int, [_p, _i64, _i64, _p, _p, _p]),
+    "pcg_update_inv_f64": (C.c_int, [_p, _p, _p, _i64, _p, _i64, _p, _p]),
     "pcg_energy_f64": (C.c_int, [_p, _pi64, _p, _pi64, _p, _p, _i64, _i64, _p, _i64, _p, _p]),
     "pcg_dots_f64": (C.c_int, [_p, C.POINTER(_p), C.c_int, _i64, _p, _i64, _p, _p]),
     "pcg_dots_f64_noalloc": (C.c_int, [_p, C.POINTER(_p), C.c_int, _i64, _p, _p]),

@@ -354,11 +354,22 @@ class CCwfn:
         return out
 
     def update_amplitudes(self, r1, r2):
-        """t1 += r1/Dia, t2 += r2/Dijab in place; returns rms = ||(r1/Dia, r2/Dijab)||_2."""
-        out = self._scalars[1:2]
-        _lib.call("pcg_update_amps_f64", _ptr(self.t1), _ptr(self.t2), _ptr(r1.contiguous()),
-                  _ptr(r2.contiguous()), _ptr(self.H.eps), self.no, self.nv, _ptr(self._work),
-                  self._work.numel(), _ptr(out), self._st())
+        """t1 += r1/Dia, t2 += r2/Dijab in place (products with the inverse denominators,
+        computed once); returns the two squared partial norms as a 2-element GPU tensor."""
+        no, nv = self.no, self.nv
+        n1 = no * nv
+        if getattr(self, "_inv", None) is None:
+            self._inv = torch.empty_like(self._amps)
+            _lib.call("pcg_inv_denominators_f64", _ptr(self.H.eps), no, nv, _ptr(self._inv),
+                      _ptr(self._inv[n1:]), self._st())
+        out = self._scalars[1:3]
+        r1 = r1.contiguous()
+        r2 = r2.contiguous()
+        _lib.call("pcg_update_inv_f64", _ptr(self.t1), _ptr(r1), _ptr(self._inv), n1,
+                  _ptr(self._work), self._work.numel(), _ptr(out), self._st())
+        _lib.call("pcg_update_inv_f64", _ptr(self.t2), _ptr(r2), _ptr(self._inv[n1:]),
+                  self._amps.numel() - n1, _ptr(self._work), self._work.numel(),
+                  _ptr(out[1:]), self._st())
         return out
 
     # -- pycc/ccwfn.py:216-319 ------------------------------------------------------------
@@ -386,8 +397,8 @@ class CCwfn:
         rms_t = self.update_amplitudes(r1, r2)
         e_t = self.cc_energy(o, v, F, L, self.t1, self.t2)
         del r1, r2
-        vals = torch.stack([e_t.reshape(()), rms_t.reshape(())]).cpu().numpy()
-        ecc, rms = float(vals[0]), math.sqrt(max(float(vals[1]), 0.0))
+        vals = torch.cat([e_t.reshape(1), rms_t.reshape(-1)]).cpu().numpy()
+        ecc, rms = float(vals[0]), math.sqrt(max(float(vals[1:].sum()), 0.0))
         if self.precision in ('MIXED', 'SP'):
             self.mixed_engine().tc.check_status()
         self.energies.append(ecc)

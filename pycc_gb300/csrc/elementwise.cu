@@ -122,6 +122,41 @@ __global__ void update_kernel(double* __restrict__ t1, double* __restrict__ t2,
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+__global__ void inv_denom_kernel(const double* __restrict__ eps, long long no, long long nv,
+                                 double* __restrict__ inv1, double* __restrict__ inv2) {
+  const long long n1 = no * nv, total = n1 + no * no * nv * nv;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (long long)gridDim.x * blockDim.x) {
+    if (idx < n1) {
+      const long long a = idx % nv, i = idx / nv;
+      inv1[idx] = 1.0 / (eps[i] - eps[no + a]);
+    } else {
+      const long long q = idx - n1;
+      long long b = q % nv, r = q / nv;
+      const long long a = r % nv;
+      r /= nv;
+      const long long j = r % no, i = r / no;
+      inv2[q] = 1.0 / (eps[i] + eps[j] - eps[no + a] - eps[no + b]);
+    }
+  }
+}
+
+// t += r * (1/D) with precomputed inverse denominators: three FP64 operations per element
+// (the divide of update_kernel costs an order of magnitude more on the FP64 pipe).
+__global__ void update_inv_kernel(double* __restrict__ t, const double* __restrict__ r,
+                                  const double* __restrict__ inv, long long n,
+                                  double* __restrict__ part) {
+  double acc = 0.0;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < n;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const double u = r[idx] * inv[idx];
+    t[idx] += u;
+    acc += u * u;
+  }
+  acc = block_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
 __global__ void energy_kernel(const double* __restrict__ fov, long long fs0, long long fs1,
                               const double* __restrict__ L, Strides4 ls,
                               const double* __restrict__ t1, const double* __restrict__ t2,
@@ -446,5 +481,37 @@ extern "C" int pcg_dots_f64_noalloc(const double* x, const double* const* ys, in
   PCG_CHECK_LAUNCH("pcg_dots_f64_noalloc/partials");
   finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(scratch, nb, k, out);
   PCG_CHECK_LAUNCH("pcg_dots_f64_noalloc");
+  return 0;
+}
+
+// inv1[i,a] = 1/(e_i - e_a), inv2[i,j,a,b] = 1/(e_i + e_j - e_a - e_b): the Jacobi
+// preconditioner of the amplitude update (pycc/ccwfn.py:195-198), computed once.
+extern "C" int pcg_inv_denominators_f64(const double* eps, long long no, long long nv,
+                                        double* inv1, double* inv2, void* stream) {
+  if (!eps || !inv1 || !inv2 || no <= 0 || nv <= 0) {
+    set_error("pcg_inv_denominators_f64: bad arguments");
+    return -1;
+  }
+  const long long n = no * nv + no * no * nv * nv;
+  inv_denom_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(eps, no, nv, inv1, inv2);
+  PCG_CHECK_LAUNCH("pcg_inv_denominators_f64");
+  return 0;
+}
+
+// t += r * inv over n elements (t1 and t2 as one flat vector when they are adjacent);
+// *rms2 = sum (r*inv)^2.  work >= 1024 doubles.  solve_cc update (pycc/ccwfn.py:281-284).
+extern "C" int pcg_update_inv_f64(double* t, const double* r, const double* inv, long long n,
+                                  double* work, long long work_len, double* rms2, void* stream) {
+  if (!t || !r || !inv || !rms2 || n < 0) {
+    set_error("pcg_update_inv_f64: bad arguments");
+    return -1;
+  }
+  if (!check_work(work_len, RED_BLOCKS, "pcg_update_inv_f64")) return -1;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nb = std::min(ew_blocks(n), RED_BLOCKS);
+  update_inv_kernel<<<nb, EW_THREADS, 0, st>>>(t, r, inv, n, work);
+  PCG_CHECK_LAUNCH("pcg_update_inv_f64/update");
+  finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, 1, rms2);
+  PCG_CHECK_LAUNCH("pcg_update_inv_f64");
   return 0;
 }

@@ -80,11 +80,14 @@ __device__ __forceinline__ long long epi_offset(const EpiIdx& d, long long r) {
 
 constexpr int kSmemMax = 232448;  // 227 KB of dynamic shared memory per CTA
 
-template <int BN>
+// NP operand pieces per stage: 1 (one product per stage; split formats run one pass per
+// product), or 2 (split-BF16x3 with both pieces of A and B in the stage, all three products
+// issued from it: a third less shared-memory fill traffic per flop).
+template <int BN, int NP = 1>
 struct Smem {
   static constexpr int A_BYTES = BM * KBYTES;
   static constexpr int B_BYTES = BN * KBYTES;
-  static constexpr int STAGE = A_BYTES + B_BYTES;
+  static constexpr int STAGE = NP * (A_BYTES + B_BYTES);
   // barriers / tmem slot / flags, then per epilogue warp BN column offsets and scales
   static constexpr int TAIL = 512 + 4 * BN * 16;
   static constexpr int FIT = (kSmemMax - 1024 - TAIL) / STAGE;
@@ -92,7 +95,7 @@ struct Smem {
   static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
   static constexpr unsigned TMEM_COLS = (2 * BN <= 128) ? 128 : ((2 * BN <= 256) ? 256 : 512);
   static_assert(BN % 32 == 0 && BN >= 64 && BN <= 256, "BN: multiple of 32 in [64, 256]");
-  static_assert(STAGES >= 3, "shared-memory ring too shallow");
+  static_assert(STAGES >= 2, "shared-memory ring too shallow");
 };
 
 // Tile t -> (split, m tile, n tile); N tiles fastest so CTAs running together share A.
@@ -111,17 +114,17 @@ __device__ __forceinline__ void decode_tile(const Args& p, long long t, int& spl
 // chunk's FP32 sum into the FP64 output while the MMA warp fills the other TMEM buffer.
 // Bounding the FP32 accumulation chain keeps the tensor-core accumulator's rounding
 // (truncating, so biased for long sums) at the level of a short dot product.
-template <int BN>
+template <int BN, int NP>
 __global__ void __launch_bounds__(NT, 1)
     tc_gemm_kernel(const __grid_constant__ Maps maps, const Args p) {
-  using L = Smem<BN>;
+  using L = Smem<BN, NP>;
   constexpr int S = L::STAGES;
   constexpr uint32_t TMEM_COLS = L::TMEM_COLS;
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw = smem_u32(smem_raw);
   uint8_t* base = smem_raw + (((raw + 1023u) & ~1023u) - raw);
-  uint8_t* sA = base;
-  uint8_t* sB = base + S * L::A_BYTES;
+  uint8_t* sA = base;                            // [stage][piece] A tiles
+  uint8_t* sB = base + S * NP * L::A_BYTES;      // [stage][piece] B tiles
   uint8_t* tail = base + S * L::STAGE;
   uint64_t* full = reinterpret_cast<uint64_t*>(tail);
   uint64_t* empty = full + S;
@@ -175,9 +178,8 @@ __global__ void __launch_bounds__(NT, 1)
         const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
         for (int c0 = kb0; c0 < kb1 && !stop; c0 += p.kb_chunk) {
           const int c1 = min(c0 + p.kb_chunk, kb1);
-          for (int pass = 0; pass < p.npass && !stop; ++pass) {
-            const CUtensorMap* ta = &maps.a[p.pt.a[pass]];
-            const CUtensorMap* tb = &maps.b[p.pt.b[pass]];
+          const int npass = (NP == 1) ? p.npass : 1;
+          for (int pass = 0; pass < npass && !stop; ++pass) {
             for (int kb = c0; kb < c1; ++kb, ++it) {
               const int s = it % S;
               if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1)) {
@@ -189,8 +191,13 @@ __global__ void __launch_bounds__(NT, 1)
                 break;
               }
               mbar_expect_tx(&full[s], L::STAGE);
-              tma_load_2d(ta, &full[s], sA + s * L::A_BYTES, kb * kelem, (int)m0);
-              tma_load_2d(tb, &full[s], sB + s * L::B_BYTES, kb * kelem, n0);
+#pragma unroll
+              for (int q = 0; q < NP; ++q) {
+                const CUtensorMap* ta = &maps.a[NP == 1 ? p.pt.a[pass] : q];
+                const CUtensorMap* tb = &maps.b[NP == 1 ? p.pt.b[pass] : q];
+                tma_load_2d(ta, &full[s], sA + (s * NP + q) * L::A_BYTES, kb * kelem, (int)m0);
+                tma_load_2d(tb, &full[s], sB + (s * NP + q) * L::B_BYTES, kb * kelem, n0);
+              }
             }
           }
         }
@@ -228,7 +235,8 @@ __global__ void __launch_bounds__(NT, 1)
           tc_fence_after();
           const uint32_t d = tmem + (uint32_t)(b * BN);
           uint32_t acc = 0u;
-          for (int pass = 0; pass < p.npass && !stop; ++pass) {
+          const int npass = (NP == 1) ? p.npass : 1;
+          for (int pass = 0; pass < npass && !stop; ++pass) {
             for (int kb = c0; kb < c1; ++kb, ++it) {
               const int s = it % S;
               if (!mbar_wait(&full[s], (it / S) & 1)) {
@@ -240,15 +248,31 @@ __global__ void __launch_bounds__(NT, 1)
                 break;
               }
               tc_fence_after();
-              const uint64_t da = sw128_desc(smem_u32(sA + s * L::A_BYTES));
-              const uint64_t db = sw128_desc(smem_u32(sB + s * L::B_BYTES));
+              if constexpr (NP == 1) {
+                const uint64_t da = sw128_desc(smem_u32(sA + s * L::A_BYTES));
+                const uint64_t db = sw128_desc(smem_u32(sB + s * L::B_BYTES));
 #pragma unroll
-              for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per 128-byte stage row
-                if (p.fp8)
-                  umma_f8(d, da + 2 * k, db + 2 * k, idesc, acc);
-                else
-                  umma_f16(d, da + 2 * k, db + 2 * k, idesc, acc);
-                acc = 1u;
+                for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per 128-byte stage row
+                  if (p.fp8)
+                    umma_f8(d, da + 2 * k, db + 2 * k, idesc, acc);
+                  else
+                    umma_f16(d, da + 2 * k, db + 2 * k, idesc, acc);
+                  acc = 1u;
+                }
+              } else {
+                // split-BF16x3 from one stage: Al.Bh, Ah.Bl, then Ah.Bh
+                const uint64_t dah = sw128_desc(smem_u32(sA + (s * NP + 0) * L::A_BYTES));
+                const uint64_t dal = sw128_desc(smem_u32(sA + (s * NP + 1) * L::A_BYTES));
+                const uint64_t dbh = sw128_desc(smem_u32(sB + (s * NP + 0) * L::B_BYTES));
+                const uint64_t dbl = sw128_desc(smem_u32(sB + (s * NP + 1) * L::B_BYTES));
+                const uint64_t prs[3][2] = {{dal, dbh}, {dah, dbl}, {dah, dbh}};
+#pragma unroll
+                for (int pr = 0; pr < 3; ++pr)
+#pragma unroll
+                  for (int k = 0; k < 4; ++k) {
+                    umma_f16(d, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc, acc);
+                    acc = 1u;
+                  }
               }
               umma_commit(&empty[s]);
             }
@@ -326,7 +350,7 @@ __global__ void __launch_bounds__(NT, 1)
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             if (co[j] < 0) continue;
-            const double v = (double)__uint_as_float(r[j]) * ascale * colsc[cc + j];
+            const double v = (double)(__uint_as_float(r[j]) * (float)(ascale * colsc[cc + j]));
             if (p.atomic_out)
               atomicAdd(crow + co[j], v);
             else
@@ -488,9 +512,16 @@ __device__ __forceinline__ double fp8_scale(unsigned maxbits) {
   return (m > 0.0) ? exp2(ceil(log2(m / 448.0))) : 1.0;
 }
 
-// FP8 pass 2: quantise with the row's power-of-two scale.
+// FP8 pass 2: replace each row's max bits by its power-of-two scale (once per row).
+__global__ void pack_fp8_scale_kernel(long long R, unsigned* rowmax_scale) {
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < R;
+       r += (long long)gridDim.x * blockDim.x)
+    reinterpret_cast<float*>(rowmax_scale)[r] = (float)fp8_scale(rowmax_scale[r]);
+}
+
+// FP8 pass 3: quantise with the row's scale (a power of two, so the FP32 product is exact).
 __global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p, int kfast,
-                                                                const unsigned* rowmax) {
+                                                                const float* scale) {
   __shared__ PackTile t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
   pack_tile_load(p, t, r0, k0, kfast);
@@ -498,16 +529,9 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p
   for (int e = threadIdx.x; e < TR * TK; e += PACK_THREADS) {
     const int rr = e / TK, kk = e % TK;
     if (r0 + rr >= p.R) continue;
-    const double inv = 1.0 / fp8_scale(rowmax[r0 + rr]);
-    dst[(r0 + rr) * p.Kp + k0 + kk] = __nv_fp8_e4m3((float)(t.v[rr][kk] * inv));
+    const float inv = 1.0f / scale[r0 + rr];
+    dst[(r0 + rr) * p.Kp + k0 + kk] = __nv_fp8_e4m3((float)t.v[rr][kk] * inv);
   }
-}
-
-// FP8 pass 3: replace each row's max bits by its scale.
-__global__ void pack_fp8_scale_kernel(long long R, unsigned* rowmax_scale) {
-  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < R;
-       r += (long long)gridDim.x * blockDim.x)
-    reinterpret_cast<float*>(rowmax_scale)[r] = (float)fp8_scale(rowmax_scale[r]);
 }
 
 __global__ void scale_epi_kernel(EpiIdx em, EpiIdx en, long long M, long long N, double beta,
@@ -572,18 +596,18 @@ int num_sms() {
   return sms;
 }
 
-template <int BN>
+template <int BN, int NP = 1>
 int launch(const Maps& maps, Args a, cudaStream_t st) {
   static bool attr = false;
-  const int smem = Smem<BN>::TOTAL;
+  const int smem = Smem<BN, NP>::TOTAL;
   if (!attr) {
-    cudaFuncSetAttribute(tc_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(tc_gemm_kernel<BN, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
   a.nt = (a.N + BN - 1) / BN;
   const long long ntiles = a.mt * a.nt * a.splits;
   const long long grid = std::min<long long>(ntiles, num_sms());
-  tc_gemm_kernel<BN><<<(unsigned)grid, NT, smem, st>>>(maps, a);
+  tc_gemm_kernel<BN, NP><<<(unsigned)grid, NT, smem, st>>>(maps, a);
   PCG_CHECK_LAUNCH("pcg_tc_gemm");
   return 0;
 }
@@ -698,9 +722,9 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
     cudaMemsetAsync(mx, 0, sizeof(float) * p.R, st);
     pack_fp8_max_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, mx);
     PCG_CHECK_LAUNCH("pcg_pack_operand/max");
-    pack_fp8_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, mx);
-    PCG_CHECK_LAUNCH("pcg_pack_operand/fp8");
     pack_fp8_scale_kernel<<<(unsigned)std::min<long long>((p.R + 255) / 256, 4096), 256, 0, st>>>(p.R, mx);
+    PCG_CHECK_LAUNCH("pcg_pack_operand/scale");
+    pack_fp8_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, row_scale);
   } else {
     pack_bf16_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast);
   }
@@ -764,9 +788,12 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.status = status;
   // tile width: least padded work, weighting each tile by its fixed A-operand share
   static const int kBN[] = {64, 96, 128, 160, 192, 224, 256};
+  static const int kBNfused[] = {64, 128, 256};
+  const bool fused = (fmt == kBF16x3);
   int BN = 64;
   long long best = -1;
   for (int bn : kBN) {
+    if (fused && bn != kBNfused[0] && bn != kBNfused[1] && bn != kBNfused[2]) continue;
     const long long tiles_n = (N + bn - 1) / bn;
     const long long cost = tiles_n * (bn + 48);
     if (best < 0 || cost < best || (cost == best && bn > BN)) {
@@ -809,6 +836,13 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   for (int q = 0; q < 3; ++q) {
     if (!make_map(&maps.a[q], pa[q] ? pa[q] : A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
     if (!make_map(&maps.b[q], pb[q] ? pb[q] : B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
+  }
+  if (fused) {
+    switch (BN) {
+      case 64: return launch<64, 2>(maps, a, st);
+      case 128: return launch<128, 2>(maps, a, st);
+      default: return launch<256, 2>(maps, a, st);
+    }
   }
   switch (BN) {
     case 64: return launch<64>(maps, a, st);

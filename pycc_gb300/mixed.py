@@ -52,6 +52,7 @@ class MixedResidual:
         self.history = []
         self.profile = None       # list of (subscripts, fmt, start, end) events when set
         self._pairs = None        # i <= j pair tables of the ladder
+        self._r_seed = None
 
     # -- precision schedule ---------------------------------------------------------------
     def select_mode(self, rms):
@@ -234,7 +235,10 @@ class MixedResidual:
         o, v = self.w.o, self.w.v
         no, nv = self.w.no, self.w.nv
         ERI = self.w.H.ERI
-        r = self.w._combine(0.5, ERI[v, v, o, o].permute(2, 3, 0, 1), 0.0, None, None)
+        if self._r_seed is None:       # 1/2 <ab|ij> in the [i,j,a,b] layout, built once
+            self._r_seed = self.w._combine(0.5, ERI[v, v, o, o].permute(2, 3, 0, 1), 0.0, None,
+                                           None, record=False)
+        r = self._r_seed.clone()
         # t2_ijae (F_be - 1/2 t_mb F_me) and - t2_imab (F_mj + 1/2 t_je F_me)
         Fbe = Fae.clone()
         contract_f64('mb,me->be', t1, Fme, out=Fbe, alpha=-0.5, beta=1.0)
@@ -267,6 +271,7 @@ class MixedResidual:
     def residuals(self, F, t1, t2):
         t1 = t1.contiguous()
         t2 = t2.contiguous()
+        self.tc.dyn_cache = {}          # identical dynamic operands are packed once per call
         Fae = self.build_Fae(F, t1, t2)
         Fmi = self.build_Fmi(F, t1, t2)
         Fme = self.build_Fme(F, t1)

@@ -184,6 +184,7 @@ class TCEngine:
         self.status = torch.zeros(4, dtype=torch.int32, device=device)
         self.cache = {}
         self.timing = None        # list of GEMM launch records (CUDA events) when set
+        self.dyn_cache = None     # per-residual cache of packed dynamic operands
 
     def cached_bytes(self):
         return sum(p.nbytes() for p in self.cache.values())
@@ -241,7 +242,16 @@ class TCEngine:
 
     def _pack(self, op, rows, ks, fmt, side):
         if op.key is None:
-            return pack(op, rows, ks, fmt, self.stream)
+            if self.dyn_cache is None:
+                return pack(op, rows, ks, fmt, self.stream)
+            src = tuple((s[0].data_ptr(), tuple(s[0].stride()), s[1]) if s is not None else None
+                        for s in op.sources())
+            dkey = (src, op.a, op.b, op.c, op.labels, tuple(rows), tuple(ks), fmt)
+            p = self.dyn_cache.get(dkey)
+            if p is None:
+                p = pack(op, rows, ks, fmt, self.stream)
+                self.dyn_cache[dkey] = p
+            return p
         # the operand's own label string fixes which tensor axis each label names
         key = (op.key, op.labels, tuple(rows), tuple(ks), fmt)
         p = self.cache.get(key)
