@@ -156,7 +156,9 @@ int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* 
 
 /* pcg_tc_gemm: C[off_m(m) + off_n(n)] = beta*C + alpha * sum_k A[m][k] B[n][k] (C FP64).
  *   A: M rows of lda elements (K-major, 16-byte aligned rows), B: N rows of ldb elements;
- *   format as above: 1 = three tcgen05 passes Al.Bh + Ah.Bl + Ah.Bh, 3 = the six piece
+ *   format as above, plus 4 = split-BF16x3 fused (both pieces of A and B loaded per stage,
+ *   the three products issued from it; faster, with a slightly larger FP32 truncation bias),
+ *   1 = three tcgen05 passes Al.Bh + Ah.Bl + Ah.Bh, 3 = the six piece
  *   products of order <= 2^-16 (smallest first), 2 = FP8 with the row scales applied in the
  *   epilogue.  off_m / off_n: flat index over up to 4 sub-indices (extents, element strides
  *   in C); col_map (optional, device, N entries) replaces off_n and col_scale (optional,

@@ -24,7 +24,7 @@
 namespace pcg {
 namespace tc {
 
-enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2, kBF16x6 = 3 };
+enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2, kBF16x6 = 3, kBF16x3F = 4 };
 
 // Operand pieces multiplied in each pass (A piece, B piece), smallest products first so
 // the FP32 accumulator sums the small corrections before the leading term.
@@ -669,6 +669,7 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   PackArgs p{};
   if (!fill_pack(p.r, r_n, r_ext, r_str) || !fill_pack(p.k, k_n, k_ext, k_str)) return -1;
   p.row_tab = row_tab;
+  if (fmt == kBF16x3F) fmt = kBF16x3;  // same operand pieces; the GEMM differs
   if (fmt < 0 || fmt > 3 || (!X && !P) || !hi || ((fmt == kBF16x3 || fmt == kBF16x6) && !lo) ||
       (fmt == kBF16x6 && !mid) || (fmt == kFP8 && !row_scale) || (P && !Q)) {
     set_error("pcg_pack_operand: bad pointers for format %d", fmt);
@@ -740,13 +741,13 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
                            const long long* n_ext, const long long* n_sc,
                            const long long* col_map, const double* col_scale, double alpha,
                            double beta, double* C, int* status, void* stream) {
-  if (fmt < 0 || fmt > 3) {
+  if (fmt < 0 || fmt > 4) {
     set_error("pcg_tc_gemm: unknown format %d", fmt);
     return -1;
   }
   const int eb = (fmt == kFP8) ? 1 : 2;
   const int kblk = KBYTES / eb;
-  const bool need_lo = (fmt == kBF16x3 || fmt == kBF16x6);
+  const bool need_lo = (fmt == kBF16x3 || fmt == kBF16x6 || fmt == kBF16x3F);
   if (!A_hi || !B_hi || !C || !status || (need_lo && (!A_lo || !B_lo)) ||
       (fmt == kBF16x6 && (!A_mid || !B_mid)) || (fmt == kFP8 && (!a_scale || !b_scale))) {
     set_error("pcg_tc_gemm: null pointer for format %d", fmt);
@@ -789,7 +790,7 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   // tile width: least padded work, weighting each tile by its fixed A-operand share
   static const int kBN[] = {64, 96, 128, 160, 192, 224, 256};
   static const int kBNfused[] = {64, 128, 256};
-  const bool fused = (fmt == kBF16x3);
+  const bool fused = (fmt == kBF16x3F);
   int BN = 64;
   long long best = -1;
   for (int bn : kBN) {
@@ -822,7 +823,9 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.nkb_total = nkb;
   a.kb_per_split = kps;
   // FP32 accumulation chain per flush: 4096 K for split-BF16x3, 2048 for BF16x6
-  a.kb_chunk = (fmt == kBF16x3) ? 64 : (fmt == kBF16x6 ? 32 : 192);
+  // FP32 accumulation chain per FP64 flush: 4096 K for split-BF16x3 (fused or by passes),
+  // 2048 K for BF16x6, 12288 K for single BF16.
+  a.kb_chunk = (fmt == kBF16x3 || fmt == kBF16x3F) ? 64 : (fmt == kBF16x6 ? 32 : 192);
   a.atomic_out = splits > 1;
   cudaStream_t st = (cudaStream_t)stream;
   if (a.atomic_out && beta != 1.0) {

@@ -22,15 +22,18 @@ import torch
 
 from . import _lib
 from .contract import contract_f64
-from .tc import FMT_BF16, FMT_BF16X3, FMT_BF16X6, FMT_FP8, Operand, TCEngine, pack
+from .tc import FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X6, FMT_FP8, Operand, TCEngine, pack
 
 
 class MixedResidual:
-    """Precision ladder: FP8 ladder + BF16 -> BF16 -> split-BF16x3.
+    """Precision ladder: FP8 ladder + BF16 -> BF16 -> split-BF16x3 fused -> split-BF16x3.
 
     A stage hands over to the next when the update norm drops below its threshold or
     stops decreasing (the stage's rounding floor): ``fp8_threshold`` (1e-3) for the FP8
-    stage, ``switch_threshold`` (1e-5) for BF16.
+    stage, ``switch_threshold`` (1e-5) for BF16.  The fused split-BF16x3 stage (all three
+    products from one shared-memory stage) runs until its floor; the last stage issues the
+    products as separate passes, whose FP32 chains carry less truncation bias, and
+    fixes the converged energy.
     """
 
     STALL_RATIO = 0.8     # rms above this fraction of the stage's best counts as no progress
@@ -44,9 +47,11 @@ class MixedResidual:
         elif mode == "bf16x3":
             self.stages = ["bf16x3"]
         else:
-            self.stages = (["fp8", "bf16", "bf16x3"] if w.vvvv_fp8 else ["bf16", "bf16x3"])
+            self.stages = (["fp8", "bf16", "bf16x3f", "bf16x3"] if w.vvvv_fp8
+                           else ["bf16", "bf16x3f", "bf16x3"])
         self.stage = 0
-        self.thresholds = {"fp8": getattr(w, "fp8_threshold", 1e-3), "bf16": w.switch_threshold}
+        self.thresholds = {"fp8": getattr(w, "fp8_threshold", 1e-3), "bf16": w.switch_threshold,
+                           "bf16x3f": 0.0}
         self.best = float("inf")
         self.bad = 0
         self.history = []
@@ -91,7 +96,8 @@ class MixedResidual:
     def mode_name(self):
         return self.stages[self.stage]
 
-    FMTS = {"bf16": FMT_BF16, "bf16x3": FMT_BF16X3, "bf16x6": FMT_BF16X6, "fp8": FMT_BF16}
+    FMTS = {"bf16": FMT_BF16, "bf16x3f": FMT_BF16X3F, "bf16x3": FMT_BF16X3, "bf16x6": FMT_BF16X6,
+            "fp8": FMT_BF16}
 
     def fmt(self):
         return self.FMTS[self.mode_name()]

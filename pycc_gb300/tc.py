@@ -20,7 +20,12 @@ import torch
 
 from . import _lib
 
-FMT_BF16, FMT_BF16X3, FMT_FP8, FMT_BF16X6 = 0, 1, 2, 3
+FMT_BF16, FMT_BF16X3, FMT_FP8, FMT_BF16X6, FMT_BF16X3F = 0, 1, 2, 3, 4
+
+
+def pack_format(fmt):
+    """The operand pieces a GEMM format reads (fused and by-pass split-BF16x3 share them)."""
+    return FMT_BF16X3 if fmt == FMT_BF16X3F else fmt
 MAX_SUB = 4
 
 
@@ -106,6 +111,7 @@ def kblock(fmt):
 def pack(op: Operand, row_labels, k_labels, fmt, stream=None, row_tab=None) -> Packed:
     """Pack ``op`` with rows over ``row_labels`` (or the explicit per-source row offsets
     ``row_tab``, an int64 [4, R] device tensor) and K over ``k_labels``."""
+    fmt = pack_format(fmt)
     ext = op.extents()
     rows = [(ext[c], op.strides(c)) for c in row_labels]
     ks = [(ext[c], op.strides(c)) for c in k_labels]
@@ -246,14 +252,14 @@ class TCEngine:
                 return pack(op, rows, ks, fmt, self.stream)
             src = tuple((s[0].data_ptr(), tuple(s[0].stride()), s[1]) if s is not None else None
                         for s in op.sources())
-            dkey = (src, op.a, op.b, op.c, op.labels, tuple(rows), tuple(ks), fmt)
+            dkey = (src, op.a, op.b, op.c, op.labels, tuple(rows), tuple(ks), pack_format(fmt))
             p = self.dyn_cache.get(dkey)
             if p is None:
                 p = pack(op, rows, ks, fmt, self.stream)
                 self.dyn_cache[dkey] = p
             return p
         # the operand's own label string fixes which tensor axis each label names
-        key = (op.key, op.labels, tuple(rows), tuple(ks), fmt)
+        key = (op.key, op.labels, tuple(rows), tuple(ks), pack_format(fmt))
         p = self.cache.get(key)
         if p is None:
             p = pack(op, rows, ks, fmt, self.stream)
