@@ -274,8 +274,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-terms", action="store_true")
-    ap.add_argument("--force-mode", default=None, choices=[None, "bf16x3"],
-                    help="start in the final precision stage (profiling of that stage)")
+    ap.add_argument("--force-mode", default=None, choices=[None, "bf16x3f", "bf16x3"],
+                    help="run every iteration in this precision stage (profiling of that stage)")
     ap.add_argument("--converge-iters", type=int, default=60,
                     help="untimed iterations allowed after the timed ones to reach the floor")
     ap.add_argument("--mode", default="ccsd", choices=["ccsd", "triples", "adjoint"],
@@ -318,7 +318,9 @@ def main():
     # ---- mixed-precision solve: W warm-up + K timed iterations ----------------------------
     w = pg.CCwfn(H, precision="MIXED")
     if args.force_mode:
-        w.mixed_engine().force_final()
+        eng0 = w.mixed_engine()
+        eng0.stage = eng0.stages.index(args.force_mode)
+        eng0.stages = eng0.stages[:eng0.stage + 1]      # hold that stage
     diis = w.start_iterations(8)
     n = 0
     for _ in range(args.warmup):
