@@ -199,6 +199,48 @@ def triples_mode(args, dev):
     print(json.dumps(line))
 
 
+def term_mode(args, dev):
+    """One contraction of the residual at full size, alone: synthetic FP64 operands with the
+    o/v extents its labels name (i-n occupied, a-h virtual), the second operand static
+    (packed once, like an integral block), the first packed on every call.  Times the pack +
+    GEMM and the GEMM launch with CUDA events; the profiling target for single kernels."""
+    import torch
+    from pycc_gb300.tc import FMT_BF16, FMT_BF16X3, FMT_BF16X3F, Operand, TCEngine
+    fmt = {"bf16": FMT_BF16, "bf16x3": FMT_BF16X3, "bf16x3f": FMT_BF16X3F}[args.term_fmt]
+    lhs, rhs = args.term.split("->")
+    la, lb = lhs.split(",")
+    ext = lambda labs: [args.no if c in "ijklmn" else args.nv for c in labs]
+    g = torch.Generator(device=dev).manual_seed(7)
+    A = torch.randn(ext(la), generator=g, dtype=torch.float64, device=dev)
+    B = torch.randn(ext(lb), generator=g, dtype=torch.float64, device=dev)
+    out = torch.randn(ext(rhs), generator=g, dtype=torch.float64, device=dev)
+    eng = TCEngine(dev)
+    opa, opb = Operand.of(la, A), Operand.of(lb, B, key=("term", lb))
+    times, gemm = [], []
+    st = torch.cuda.current_stream()
+    for it in range(args.warmup + args.steps):
+        eng.timing = []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        eng.contract(args.term, opa, opb, out, fmt=fmt)
+        e1.record(st)
+        torch.cuda.synchronize()
+        if it >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+            gemm.append(eng.timing[0]["start"].elapsed_time(eng.timing[0]["end"]))
+    eng.check_status()
+    rec = eng.timing[0]
+    ms = sorted(gemm)[len(gemm) // 2]
+    c_bytes = 2 * out.numel() * 8                  # read-modify-write of the FP64 output
+    op_bytes = 4 * (rec["M"] + rec["N"]) * rec["Kp"]  # hi + lo BF16 pieces
+    print(json.dumps({"mode": "term", "term": args.term, "fmt": args.term_fmt, "no": args.no,
+                      "nv": args.nv, "M": rec["M"], "N": rec["N"], "Kp": rec["Kp"],
+                      "ms_gemm": ms, "ms_pack_gemm": sorted(times)[len(times) // 2],
+                      "hbm_gbs_gemm": (c_bytes + op_bytes) / (ms * 1e-3) / 1e9,
+                      "c_bytes": c_bytes, "operand_bytes": op_bytes,
+                      "device_gb": torch.cuda.max_memory_allocated(dev) / 1e9}))
+
+
 def adjoint_mode(args, dev, directions=16):
     """Adjoint at no=20, nv=180 (seed 3, matched coupling): Lambda + gradient densities,
     backward/forward cost, central finite differences along random symmetric directions."""
@@ -278,9 +320,12 @@ def main():
                     help="run every iteration in this precision stage (profiling of that stage)")
     ap.add_argument("--converge-iters", type=int, default=60,
                     help="untimed iterations allowed after the timed ones to reach the floor")
-    ap.add_argument("--mode", default="ccsd", choices=["ccsd", "triples", "adjoint"],
+    ap.add_argument("--mode", default="ccsd", choices=["ccsd", "triples", "adjoint", "term"],
                     help="ccsd: the benchmark line; triples / adjoint: the (T) and adjoint "
-                         "measurements at no=30,nv=240 and no=20,nv=180")
+                         "measurements at no=30,nv=240 and no=20,nv=180; term: one residual "
+                         "contraction (--term) alone at --no/--nv")
+    ap.add_argument("--term", default="nb,mnej->mbej")
+    ap.add_argument("--term-fmt", default="bf16x3f", choices=["bf16", "bf16x3", "bf16x3f"])
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -290,7 +335,7 @@ def main():
         import torch
         dev = torch.device("cuda:%d" % local)
         torch.cuda.set_device(dev)
-        (triples_mode if args.mode == "triples" else adjoint_mode)(args, dev)
+        {"triples": triples_mode, "adjoint": adjoint_mode, "term": term_mode}[args.mode](args, dev)
         return
 
     import numpy as np

@@ -36,6 +36,40 @@ __host__ __device__ inline void sub_offsets(const SubIdx& d, long long r, long l
   }
 }
 
+// FP64 -> FP32, rounded to nearest even, in integer arithmetic.  GB300 issues FP64
+// instructions (conversions from FP64 included) at a small fraction of its FP32 and integer
+// rates, so streaming kernels that only need FP32 accuracy read FP64 data through this.
+// Magnitudes below FP32's normal range flush to zero; above it, infinity; NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(u >> 32), lo = (unsigned)u;
+  const unsigned ex = (hi >> 20) & 0x7ffu;
+  const int e = (int)ex - (1023 - 127);
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of the 52 mantissa bits
+  const unsigned rest = lo & 0x1fffffffu;                  // the 29 bits dropped
+  unsigned f = ((unsigned)e << 23) + m;
+  f += (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) ? 1u : 0u;
+  if (e <= 0) f = 0u;
+  if (e >= 255) f = (ex == 0x7ffu && ((hi & 0xfffffu) | lo)) ? 0x7fc00000u : 0x7f800000u;
+  return __uint_as_float((hi & 0x80000000u) | f);
+}
+
+// FP32 -> FP64 (exact) in integer arithmetic, for the same reason.  FP32 subnormals, which
+// an FP32 accumulator of this library's magnitudes does not produce, flush to zero.
+__device__ __forceinline__ double f32_to_f64(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  unsigned hi = u & 0x80000000u, lo = 0u;
+  if (e == 0xffu) {
+    hi |= 0x7ff00000u | ((u & 0x7fffffu) >> 3);
+    lo = u << 29;
+  } else if (e != 0u) {
+    hi |= ((e + (1023u - 127u)) << 20) | ((u & 0x7fffffu) >> 3);
+    lo = u << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
 inline long long sub_total(const SubIdx& d) {
   long long t = 1;
   for (int q = 0; q < d.n; ++q) t *= d.ext[q];

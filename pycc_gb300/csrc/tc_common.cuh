@@ -9,7 +9,7 @@ namespace tc {
 
 constexpr int BM = 128;
 constexpr int KBYTES = 128;            // bytes of K per stage row (one 128B swizzle span)
-constexpr int NT = 192;          // warp 0: TMA, warp 1: MMA, warps 2..5: epilogue
+constexpr int NT = 192;          // grouped GEMM: warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int EPI_THREADS = 128;
 constexpr unsigned long long kWaitNs = 4000000000ull;  // 4 s bound on any single wait
 
@@ -122,6 +122,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+      "%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
 
 // host helpers (tc_gemm.cu)
 bool make_map(CUtensorMap* m, const void* base, long long rows, long long ld_bytes,

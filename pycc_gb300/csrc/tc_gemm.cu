@@ -12,8 +12,9 @@
 // * Mainloop: one CTA computes a 128 x BN FP32 tile in TMEM.  Warp 0 lane 0 issues TMA
 //   (cp.async.bulk.tensor, 128B swizzle) into an S-stage shared-memory ring; warp 1
 //   lane 0 issues tcgen05.mma (kind::f16 or kind::f8f6f4) and releases stages with
-//   tcgen05.commit; all four warps then drain TMEM (tcgen05.ld 32x32b) and write FP64
-//   with the output permutation folded into per-row / per-column offsets.
+//   tcgen05.commit; eight epilogue warps (two per TMEM lane quarter, one per column half)
+//   drain TMEM (tcgen05.ld 32x32b) and write FP64 with the output permutation folded into
+//   per-row / per-column offsets.
 // * Every mbarrier wait is bounded (globaltimer); on expiry the CTA records a status code
 //   in a caller-provided device word, stops issuing work and releases its TMEM.
 #include "tc_common.cuh"
@@ -68,17 +69,28 @@ struct Args {
   int* status;
 };
 
+// Offset of output row (or column) r: r and the extents are below 2^31 (the host checks
+// M, N against the TMA coordinate range), so the decomposition runs in 32-bit integer
+// arithmetic instead of the much longer 64-bit division sequence.
 __device__ __forceinline__ long long epi_offset(const EpiIdx& d, long long r) {
   long long o = 0;
+  unsigned x = (unsigned)r;
   for (int q = d.n - 1; q >= 0; --q) {
-    long long e = d.ext[q];
-    o += (r % e) * d.s[q];
-    r /= e;
+    const unsigned e = (unsigned)d.ext[q];
+    o += (long long)(x % e) * d.s[q];
+    x /= e;
   }
   return o;
 }
 
 constexpr int kSmemMax = 232448;  // 227 KB of dynamic shared memory per CTA
+
+// Warp roles: warp 0 issues TMA, warp 1 issues tcgen05.mma, warps 2..9 drain TMEM.  Two
+// epilogue warps share each TMEM lane quarter (warp w reads lanes 32 (w % 4) ..), one per
+// half of the tile's columns: with one warp per scheduler the FP64 read-modify-write of a
+// short-K GEMM is bound by instruction latency, two overlap it.
+constexpr int GEMM_EPI_WARPS = 8;
+constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI_WARPS;
 
 // NP operand pieces per stage: 1 (one product per stage; split formats run one pass per
 // product), or 2 (split-BF16x3 with both pieces of A and B in the stage, all three products
@@ -88,8 +100,8 @@ struct Smem {
   static constexpr int A_BYTES = BM * KBYTES;
   static constexpr int B_BYTES = BN * KBYTES;
   static constexpr int STAGE = NP * (A_BYTES + B_BYTES);
-  // barriers / tmem slot / flags, then per epilogue warp BN column offsets and scales
-  static constexpr int TAIL = 512 + 4 * BN * 16;
+  // barriers / tmem slot / flags, then per epilogue warp BN/2 column offsets and scales
+  static constexpr int TAIL = 512 + GEMM_EPI_WARPS * (BN / 2) * 12;
   static constexpr int FIT = (kSmemMax - 1024 - TAIL) / STAGE;
   static constexpr int STAGES = FIT > 8 ? 8 : FIT;
   static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
@@ -108,6 +120,52 @@ __device__ __forceinline__ void decode_tile(const Args& p, long long t, int& spl
   n0 = (r % p.nt);
 }
 
+// One batch of W (16 or 32) accumulator columns of this thread's output row: every old C
+// value of the batch is loaded before any store (W independent requests in flight per
+// thread).  Scales are
+// FP32 (powers of two and the terms' small factors) and the widening is integer
+// arithmetic, so the only FP64 instruction per element is the accumulate into C.
+// Tile column of the jj-th column drained by the epilogue warp of column half h: 32-column
+// blocks alternate between the two halves and an odd last block is split 16 / 16, so every
+// tcgen05.ld starts at a multiple of its own width (32 or 16 columns).
+template <int BN>
+__device__ __forceinline__ int epi_col(int h, int jj) {
+  constexpr int NB = BN / 32, NFULL = NB / 2;
+  if (jj < 32 * NFULL) return 32 * (2 * (jj >> 5) + h) + (jj & 31);
+  return 32 * (NB - 1) + 16 * h + (jj - 32 * NFULL);
+}
+
+template <int W>
+__device__ __forceinline__ void epi_batch(uint32_t taddr, const long long* co, const float* sc,
+                                          bool row_ok, double* crow, float ascale,
+                                          double cscale, bool need_old, int atomic_out) {
+  uint32_t r[W];
+  if constexpr (W == 32) tmem_ld32(taddr, r);
+  else tmem_ld16(taddr, r);
+  if (!row_ok) return;
+  double old[W];
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    const long long c = co[j];
+    old[j] = (need_old && c >= 0) ? crow[c] : 0.0;
+  }
+  // the offsets are read again from shared memory rather than held in registers across
+  // the loads (r and old already take 3 W of the thread's registers)
+  const volatile long long* cov = co;
+#pragma unroll
+  for (int j = 0; j < W; ++j) {
+    const long long c = cov[j];
+    if (c < 0) continue;
+    const double v = f32_to_f64(__uint_as_float(r[j]) * (ascale * sc[j]));
+    if (atomic_out)
+      atomicAdd(crow + c, v);
+    else if (cscale == 1.0)
+      crow[c] = old[j] + v;
+    else
+      crow[c] = fma(cscale, old[j], v);
+  }
+}
+
 // Persistent, warp-specialised tcgen05 GEMM.  Each CTA walks the tiles t = blockIdx.x,
 // blockIdx.x + gridDim.x, ...; each tile's K range is cut into chunks of kb_chunk K blocks
 // (all passes of a chunk accumulate into one TMEM buffer), and the epilogue warps add each
@@ -115,7 +173,7 @@ __device__ __forceinline__ void decode_tile(const Args& p, long long t, int& spl
 // Bounding the FP32 accumulation chain keeps the tensor-core accumulator's rounding
 // (truncating, so biased for long sums) at the level of a short dot product.
 template <int BN, int NP>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ Maps maps, const Args p) {
   using L = Smem<BN, NP>;
   constexpr int S = L::STAGES;
@@ -133,8 +191,9 @@ __global__ void __launch_bounds__(NT, 1)
   uint64_t* mdone = tempty + 2;  // all MMAs of this CTA retired
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-  long long* colofs_all = reinterpret_cast<long long*>(tail + 512);  // [4 warps][BN]
-  double* colsc_all = reinterpret_cast<double*>(tail + 512 + 4 * BN * 8);  // [4 warps][BN]
+  constexpr int HB = BN / 2;  // columns drained by one epilogue warp
+  long long* colofs_all = reinterpret_cast<long long*>(tail + 512);  // [8 warps][HB]
+  float* colsc_all = reinterpret_cast<float*>(tail + 512 + GEMM_EPI_WARPS * HB * 8);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long ntiles = p.mt * p.nt * p.splits;
@@ -147,7 +206,7 @@ __global__ void __launch_bounds__(NT, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], EPI_THREADS / 32);
+      mbar_init(&tempty[b], GEMM_EPI_WARPS);
     }
     mbar_init(mdone, 1);
     *abort_flag = 0;
@@ -286,9 +345,10 @@ __global__ void __launch_bounds__(NT, 1)
     __syncwarp();
   } else {
     // ---- epilogue warps: TMEM -> registers -> FP64 C, one chunk at a time ----
-    const int q = warp & 3;  // the TMEM lane quarter this warp may read
-    long long* colofs = colofs_all + (warp - 2) * BN;  // this warp's copy
-    double* colsc = colsc_all + (warp - 2) * BN;
+    const int q = warp & 3;         // the TMEM lane quarter this warp may read
+    const int h = (warp - 2) >> 2;  // the half of the tile's columns it drains
+    long long* colofs = colofs_all + (warp - 2) * HB;
+    float* colsc = colsc_all + (warp - 2) * HB;
     int u = 0;
     bool stop = false;
     for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
@@ -301,16 +361,16 @@ __global__ void __launch_bounds__(NT, 1)
       const long long row = m0 + q * 32 + lane;
       const bool row_ok = row < p.M;
       const long long roff = row_ok ? epi_offset(p.em, row) : 0;
-      const double ascale = (p.fp8 && row_ok) ? (double)p.a_scale[row] : 1.0;
+      const float ascale = (p.fp8 && row_ok) ? p.a_scale[row] : 1.0f;
       __syncwarp();  // the previous tile's column offsets are no longer read
-      for (int j = lane; j < BN; j += 32) {
-        const long long c = n0 + j;
+      for (int j = lane; j < HB; j += 32) {
+        const long long c = n0 + epi_col<BN>(h, j);
         const bool in = c < p.N;
         colofs[j] = in ? (p.col_map ? p.col_map[c] : epi_offset(p.en, c)) : -1;
         double sc = p.alpha;
         if (in && p.fp8) sc *= (double)p.b_scale[c];
         if (in && p.col_scale) sc *= p.col_scale[c];
-        colsc[j] = sc;
+        colsc[j] = (float)sc;
       }
       __syncwarp();
       bool first = true;
@@ -335,28 +395,15 @@ __global__ void __launch_bounds__(NT, 1)
         const double cscale = first ? p.beta : 1.0;  // beta applies once per tile
         const bool need_old = !p.atomic_out && cscale != 0.0;
         double* crow = p.C + roff;
+        const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
+        constexpr int NFULL = BN / 64;  // whole 32-column blocks per warp
 #pragma unroll 1
-        for (int cc = 0; cc < BN; cc += 32) {
-          uint32_t r[32];
-          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + cc), r);
-          if (!row_ok) continue;
-          long long co[32];
-          double old[32];
-#pragma unroll
-          for (int j = 0; j < 32; ++j) co[j] = colofs[cc + j];
-          // all loads of the batch before any store: 32 independent requests in flight
-#pragma unroll
-          for (int j = 0; j < 32; ++j) old[j] = (need_old && co[j] >= 0) ? crow[co[j]] : 0.0;
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            if (co[j] < 0) continue;
-            const double v = (double)(__uint_as_float(r[j]) * (float)(ascale * colsc[cc + j]));
-            if (p.atomic_out)
-              atomicAdd(crow + co[j], v);
-            else
-              crow[co[j]] = cscale * old[j] + v;
-          }
-        }
+        for (int fb = 0; fb < NFULL; ++fb)
+          epi_batch<32>(tbase + 32 * (2 * fb + h), colofs + 32 * fb, colsc + 32 * fb, row_ok,
+                        crow, ascale, cscale, need_old, p.atomic_out);
+        if constexpr (BN % 64 != 0)  // BN = 96, 160, 224: the last block split 16 / 16
+          epi_batch<16>(tbase + (BN - 32) + 16 * h, colofs + 32 * NFULL, colsc + 32 * NFULL,
+                        row_ok, crow, ascale, cscale, need_old, p.atomic_out);
         first = false;
         tc_fence_before();
         __syncwarp();
@@ -382,12 +429,15 @@ struct PackIdx {
   long long s[4][kMaxSub];  // strides of sources X, Y, P, Q
 };
 
+// Offsets of flat row (or K) index r in the four sources; r and the extents are below 2^31
+// (checked by the host), so the decomposition is 32-bit integer arithmetic.
 __device__ __forceinline__ void pack_offsets(const PackIdx& d, long long r, long long (&o)[4]) {
   o[0] = o[1] = o[2] = o[3] = 0;
+  unsigned rr = (unsigned)r;
   for (int q = d.n - 1; q >= 0; --q) {
-    long long e = d.ext[q];
-    long long x = r % e;
-    r /= e;
+    const unsigned e = (unsigned)d.ext[q];
+    const long long x = rr % e;
+    rr /= e;
     o[0] += x * d.s[0][q];
     o[1] += x * d.s[1][q];
     o[2] += x * d.s[2][q];
@@ -411,29 +461,32 @@ struct PackArgs {
   int fmt;
 };
 
-__device__ __forceinline__ double pack_value(const PackArgs& p, const long long (&ro)[4],
-                                             long long k) {
-  long long ko[4];
-  pack_offsets(p.k, k, ko);
-  double v = p.X ? p.a * p.X[ro[0] + ko[0]] : 0.0;
-  if (p.Y) v += p.b * p.Y[ro[1] + ko[1]];
-  if (p.P) v += p.c * p.P[ro[2] + ko[2]] * p.Q[ro[3] + ko[3]];
-  return v;
-}
-
 // Tiled pack: a block handles TR rows x TK columns of K.  Row and column offsets of the
 // four sources are decomposed once per tile into shared memory; values are gathered along
 // whichever index is unit-stride in X (kfast) and written out along K, so both the FP64
-// reads and the packed writes are coalesced.
-constexpr int TR = 32, TK = 64, PACK_THREADS = 256;
+// reads and the packed writes are coalesced.  The value type V is double for BF16x6 (three
+// pieces carry 24 bits) and float otherwise: FP64 inputs are rounded to FP32 in integer
+// arithmetic (f64_to_f32) and combined and split in FP32, which keeps the kernel a stream
+// instead of a loop on GB300's FP64 pipe.  A BF16 hi/lo pair holds 16 bits, so the FP32
+// rounding (2^-24 of the operands) is far below the split's own error.
+constexpr int TR = 64, TK = 64, PACK_THREADS = 256;
+static_assert((TR * TK) % PACK_THREADS == 0, "pack tile: whole elements per thread");
 
+template <typename V>
 struct PackTile {
   long long rof[4][TR];
   long long kof[4][TK];
-  double v[TR][TK + 1];
+  V v[TR][TK + 1];
 };
 
-__device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile& t, long long r0,
+template <typename V>
+__device__ __forceinline__ V pack_ld(const double* q) {
+  if constexpr (sizeof(V) == sizeof(double)) return *q;
+  else return f64_to_f32(*q);
+}
+
+template <typename V>
+__device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t, long long r0,
                                                long long k0, int kfast) {
   const int tid = threadIdx.x;
   if (tid < TR) {
@@ -445,29 +498,64 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile& t, l
         pack_offsets(p.r, r0 + tid, o);
     }
     for (int s = 0; s < 4; ++s) t.rof[s][tid] = o[s];
-  } else if (tid >= 64 && tid < 64 + TK) {
-    const int j = tid - 64;
+  } else if (tid >= TR && tid < TR + TK) {
+    const int j = tid - TR;
     long long o[4] = {0, 0, 0, 0};
     if (k0 + j < p.K) pack_offsets(p.k, k0 + j, o);
     for (int s = 0; s < 4; ++s) t.kof[s][j] = o[s];
   }
   __syncthreads();
-  for (int e = tid; e < TR * TK; e += PACK_THREADS) {
+  const V a = (V)p.a, b = (V)p.b, c = (V)p.c;
+  // all of a thread's gathers are issued before the first shared-memory store
+  constexpr int PER = TR * TK / PACK_THREADS;
+  V vals[PER];
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int e = tid + u * PACK_THREADS;
     int rr, kk;
     if (kfast) { rr = e / TK; kk = e % TK; } else { kk = e / TR; rr = e % TR; }
-    double v = 0.0;
+    V v = 0;
     if (r0 + rr < p.R && k0 + kk < p.K) {
-      v = p.X ? p.a * p.X[t.rof[0][rr] + t.kof[0][kk]] : 0.0;
-      if (p.Y) v += p.b * p.Y[t.rof[1][rr] + t.kof[1][kk]];
-      if (p.P) v += p.c * p.P[t.rof[2][rr] + t.kof[2][kk]] * p.Q[t.rof[3][rr] + t.kof[3][kk]];
+      if (p.X) v = a * pack_ld<V>(p.X + t.rof[0][rr] + t.kof[0][kk]);
+      if (p.Y) v += b * pack_ld<V>(p.Y + t.rof[1][rr] + t.kof[1][kk]);
+      if (p.P)
+        v += c * pack_ld<V>(p.P + t.rof[2][rr] + t.kof[2][kk]) *
+             pack_ld<V>(p.Q + t.rof[3][rr] + t.kof[3][kk]);
     }
-    t.v[rr][kk] = v;
+    vals[u] = v;
+  }
+#pragma unroll
+  for (int u = 0; u < PER; ++u) {
+    const int e = tid + u * PACK_THREADS;
+    int rr, kk;
+    if (kfast) { rr = e / TK; kk = e % TK; } else { kk = e / TR; rr = e % TR; }
+    t.v[rr][kk] = vals[u];
   }
   __syncthreads();
 }
 
+// BF16 / split-BF16x3 from an FP32 tile: two adjacent K entries per thread, written as one
+// bf16x2 word (K offsets are even: Kp and k0 are multiples of 64).
 __global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs p, int kfast) {
-  __shared__ PackTile t;
+  __shared__ PackTile<float> t;
+  const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
+  pack_tile_load(p, t, r0, k0, kfast);
+  __nv_bfloat162* hi = reinterpret_cast<__nv_bfloat162*>(p.hi);
+  __nv_bfloat162* lo = reinterpret_cast<__nv_bfloat162*>(p.lo);
+  for (int e = threadIdx.x; e < TR * TK / 2; e += PACK_THREADS) {
+    const int rr = e / (TK / 2), kk = 2 * (e % (TK / 2));
+    if (r0 + rr >= p.R) continue;
+    const long long at = ((r0 + rr) * p.Kp + k0 + kk) >> 1;
+    const float v0 = t.v[rr][kk], v1 = t.v[rr][kk + 1];
+    const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+    hi[at] = h;
+    if (lo) lo[at] = __floats2bfloat162_rn(v0 - __low2float(h), v1 - __high2float(h));
+  }
+}
+
+// Split-BF16x6 (hi, mid, lo) from an FP64 tile.
+__global__ void __launch_bounds__(PACK_THREADS) pack_bf16x6_kernel(const PackArgs p, int kfast) {
+  __shared__ PackTile<double> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
   pack_tile_load(p, t, r0, k0, kfast);
   __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(p.hi);
@@ -481,12 +569,10 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs 
     const __nv_bfloat16 h = __double2bfloat16(v);
     hi[at] = h;
     double rest = v - (double)__bfloat162float(h);
-    if (mid) {
-      const __nv_bfloat16 m = __double2bfloat16(rest);
-      mid[at] = m;
-      rest -= (double)__bfloat162float(m);
-    }
-    if (lo) lo[at] = __double2bfloat16(rest);
+    const __nv_bfloat16 m = __double2bfloat16(rest);
+    mid[at] = m;
+    rest -= (double)__bfloat162float(m);
+    lo[at] = __double2bfloat16(rest);
   }
 }
 
@@ -494,15 +580,15 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs 
 // unsigned order of the bits is the float order).
 __global__ void __launch_bounds__(PACK_THREADS) pack_fp8_max_kernel(const PackArgs p, int kfast,
                                                                     unsigned* rowmax) {
-  __shared__ PackTile t;
+  __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
   pack_tile_load(p, t, r0, k0, kfast);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int rr = warp; rr < TR; rr += PACK_THREADS / 32) {
-    double m = fmax(fabs(t.v[rr][lane]), fabs(t.v[rr][lane + 32]));
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0 && r0 + rr < p.R && m > 0.0)
-      atomicMax(rowmax + r0 + rr, __float_as_uint((float)m));
+    float m = fmaxf(fabsf(t.v[rr][lane]), fabsf(t.v[rr][lane + 32]));
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && r0 + rr < p.R && m > 0.0f)
+      atomicMax(rowmax + r0 + rr, __float_as_uint(m));
   }
 }
 
@@ -522,7 +608,7 @@ __global__ void pack_fp8_scale_kernel(long long R, unsigned* rowmax_scale) {
 // FP8 pass 3: quantise with the row's scale (a power of two, so the FP32 product is exact).
 __global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p, int kfast,
                                                                 const float* scale) {
-  __shared__ PackTile t;
+  __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
   pack_tile_load(p, t, r0, k0, kfast);
   __nv_fp8_e4m3* dst = reinterpret_cast<__nv_fp8_e4m3*>(p.hi);
@@ -530,7 +616,7 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p
     const int rr = e / TK, kk = e % TK;
     if (r0 + rr >= p.R) continue;
     const float inv = 1.0f / scale[r0 + rr];
-    dst[(r0 + rr) * p.Kp + k0 + kk] = __nv_fp8_e4m3((float)t.v[rr][kk] * inv);
+    dst[(r0 + rr) * p.Kp + k0 + kk] = __nv_fp8_e4m3(t.v[rr][kk] * inv);
   }
 }
 
@@ -607,7 +693,7 @@ int launch(const Maps& maps, Args a, cudaStream_t st) {
   a.nt = (a.N + BN - 1) / BN;
   const long long ntiles = a.mt * a.nt * a.splits;
   const long long grid = std::min<long long>(ntiles, num_sms());
-  tc_gemm_kernel<BN, NP><<<(unsigned)grid, NT, smem, st>>>(maps, a);
+  tc_gemm_kernel<BN, NP><<<(unsigned)grid, GEMM_THREADS, smem, st>>>(maps, a);
   PCG_CHECK_LAUNCH("pcg_tc_gemm");
   return 0;
 }
@@ -623,8 +709,8 @@ bool fill_epi(EpiIdx& d, int n, const long long* ext, const long long* s, const 
     d.s[0] = 0;
   }
   for (int q = 0; q < n; ++q) {
-    if (ext[q] <= 0) {
-      set_error("pcg_tc_gemm: %s extent must be positive", what);
+    if (ext[q] <= 0 || ext[q] > 0x7fffffffLL) {
+      set_error("pcg_tc_gemm: %s extent must be in [1, 2^31)", what);
       return false;
     }
     d.ext[q] = ext[q];
@@ -644,8 +730,8 @@ bool fill_pack(PackIdx& d, int n, const long long* ext, const long long* str) {
     for (int s = 0; s < 4; ++s) d.s[s][q] = 0;
   }
   for (int q = 0; q < n; ++q) {
-    if (ext[q] <= 0) {
-      set_error("pcg_pack_operand: extent must be positive");
+    if (ext[q] <= 0 || ext[q] > 0x7fffffffLL) {
+      set_error("pcg_pack_operand: extent must be in [1, 2^31)");
       return false;
     }
     d.ext[q] = ext[q];
@@ -712,7 +798,7 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
     if (p.r.s[0][q] != 0) rs = (rs == 0) ? llabs(p.r.s[0][q]) : std::min(rs, llabs(p.r.s[0][q]));
   const int kfast = (rs == 0 || (ks != 0 && ks <= rs)) ? 1 : 0;
   const long long gx = (p.R + TR - 1) / TR, gy = Kp / TK;
-  if (gy > 65535 || gx > 0x7fffffffLL) {
+  if (gy > 65535 || p.R > 0x7fffffffLL - TR) {  // row and K indices stay below 2^31
     set_error("pcg_pack_operand: operand too large (%lld x %lld)", p.R, Kp);
     return -1;
   }
@@ -726,6 +812,8 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
     pack_fp8_scale_kernel<<<(unsigned)std::min<long long>((p.R + 255) / 256, 4096), 256, 0, st>>>(p.R, mx);
     PCG_CHECK_LAUNCH("pcg_pack_operand/scale");
     pack_fp8_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, row_scale);
+  } else if (fmt == kBF16x6) {
+    pack_bf16x6_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast);
   } else {
     pack_bf16_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast);
   }
@@ -822,7 +910,6 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.splits = splits;
   a.nkb_total = nkb;
   a.kb_per_split = kps;
-  // FP32 accumulation chain per flush: 4096 K for split-BF16x3, 2048 for BF16x6
   // FP32 accumulation chain per FP64 flush: 4096 K for split-BF16x3 (fused or by passes),
   // 2048 K for BF16x6, 12288 K for single BF16.
   a.kb_chunk = (fmt == kBF16x3 || fmt == kBF16x3F) ? 64 : (fmt == kBF16x6 ? 32 : 192);

@@ -22,7 +22,8 @@ import torch
 
 from . import _lib
 from .contract import contract_f64
-from .tc import FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X6, FMT_FP8, Operand, TCEngine, pack
+from .tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X6, FMT_FP8, Operand, TCEngine, pack,
+                 pack_format)
 
 
 class MixedResidual:
@@ -76,12 +77,24 @@ class MixedResidual:
                     self._advance()
         if rms == 0.0:                      # explicit request for the final stage
             self.stage = len(self.stages) - 1
+            self._prune()
         self.history.append(self.mode_name())
 
     def _advance(self):
         self.stage = min(self.stage + 1, len(self.stages) - 1)
         self.best = float("inf")
         self.bad = 0
+        self._prune()
+
+    def _prune(self):
+        """Free the packed integrals of formats no remaining stage reads."""
+        used = set()
+        for name in self.stages[self.stage:]:
+            used.add(pack_format(self.FMTS[name]))
+            if name == "fp8":
+                used.add(FMT_FP8)
+        for key in [k for k in self.tc.cache if k[-1] not in used]:
+            del self.tc.cache[key]
 
     def at_floor(self):
         """True once the final stage has stopped reducing the update norm."""
@@ -89,6 +102,7 @@ class MixedResidual:
 
     def force_final(self):
         self.stage = len(self.stages) - 1
+        self._prune()
 
     def is_final_mode(self):
         return self.stage == len(self.stages) - 1
@@ -168,7 +182,7 @@ class MixedResidual:
         o, v = self.w.o, self.w.v
         Fae = F[v, v].clone()
         contract_f64('me,ma->ae', F[o, v], t1, out=Fae, alpha=-0.5, beta=1.0)
-        contract_f64('mf,mafe->ae', t1, self.w.H.L[o, v, v, v], out=Fae, beta=1.0)
+        self.tcc('mf,mafe->ae', Operand.of('mf', t1), self.ll('ovvv', 'mafe'), Fae)
         taut = Operand('mnaf', (t2, 'mnaf'), P=(t1, 'ma'), Q=(t1, 'nf'), c=0.5)
         self.tcc('mnaf,mnef->ae', taut, self.ll('oovv', 'mnef'), Fae, alpha=-1.0)
         return Fae
@@ -177,7 +191,7 @@ class MixedResidual:
         o, v = self.w.o, self.w.v
         Fmi = F[o, o].clone()
         contract_f64('ie,me->mi', t1, F[o, v], out=Fmi, alpha=0.5, beta=1.0)
-        contract_f64('ne,mnie->mi', t1, self.w.H.L[o, o, o, v], out=Fmi, beta=1.0)
+        self.tcc('ne,mnie->mi', Operand.of('ne', t1), self.ll('ooov', 'mnie'), Fmi)
         taut = Operand('inef', (t2, 'inef'), P=(t1, 'ie'), Q=(t1, 'nf'), c=0.5)
         self.tcc('inef,mnef->mi', taut, self.ll('oovv', 'mnef'), Fmi)
         return Fmi
@@ -185,7 +199,7 @@ class MixedResidual:
     def build_Fme(self, F, t1):
         o, v = self.w.o, self.w.v
         Fme = F[o, v].clone()
-        contract_f64('nf,mnef->me', t1, self.w.H.L[o, o, v, v], out=Fme, beta=1.0)
+        self.tcc('nf,mnef->me', Operand.of('nf', t1), self.ll('oovv', 'mnef'), Fme)
         return Fme
 
     def build_Wmnij(self, t1, t2):
@@ -217,10 +231,14 @@ class MixedResidual:
         return W
 
     def build_Zmbij(self, t1, t2):
-        no, nv = self.w.no, self.w.nv
-        Z = torch.empty((no, nv, no, no), dtype=torch.float64, device=t2.device)
+        """Z_mbij + <mb|ij> + t_ie <mb|ej> + t_je <mb|ie>: every o^3 v tensor the residual
+        contracts with t_ma, summed so that one GEMM applies them (see r_T2_half)."""
+        o, v = self.w.o, self.w.v
+        Z = self.w._combine(1.0, self.w.H.ERI[o, v, o, o], 0.0, None, None, record=False)
         tau = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
-        self.tcc('mbef,ijef->mbij', self.eri('ovvv', 'mbef'), tau, Z, beta=0.0)
+        self.tcc('mbef,ijef->mbij', self.eri('ovvv', 'mbef'), tau, Z)
+        self.tcc('ie,mbej->mbij', Operand.of('ie', t1), self.eri('ovvo', 'mbej'), Z)
+        self.tcc('je,mbie->mbij', Operand.of('je', t1), self.eri('ovov', 'mbie'), Z)
         return Z
 
     # -- residuals (pycc/ccwfn.py:718-945) ------------------------------------------------
@@ -231,7 +249,7 @@ class MixedResidual:
         contract_f64('mi,ma->ia', Fmi, t1, out=r, alpha=-1.0, beta=1.0)
         t2s = Operand('imae', (t2, 'imae'), a=2.0, Y=(t2, 'imea'), b=-1.0)
         self.tcc('imae,me->ia', t2s, Operand.of('me', Fme), r)
-        contract_f64('nf,nafi->ia', t1, self.w.H.L[o, v, v, o], out=r, beta=1.0)
+        self.tcc('nf,nafi->ia', Operand.of('nf', t1), self.ll('ovvo', 'nafi'), r)
         t2s = Operand('mief', (t2, 'mief'), a=2.0, Y=(t2, 'mife'), b=-1.0)
         self.tcc('mief,maef->ia', t2s, self.eri('ovvv', 'maef'), r)
         self.tcc('mnae,nmei->ia', Operand.of('mnae', t2), self.ll('oovo', 'nmei'), r, alpha=-1.0)
@@ -256,6 +274,9 @@ class MixedResidual:
         tau_mn = Operand('mnab', (t2, 'mnab'), P=(t1, 'ma'), Q=(t1, 'nb'), c=1.0)
         self.tcc('mnab,mnij->ijab', tau_mn, Operand.of('mnij', Wmnij), r, alpha=0.5)
         self.ladder_pairs(t1, t2, r, self.ladder_fmt())
+        # - t_ma (Z_mbij + <mb|ij>) - t_ie t_ma <mb|ej> - t_ie t_mb <ma|je>, the last written
+        # as its (i<->j, a<->b) image - t_je t_ma <mb|ie>, which the symmetrisation
+        # r2 = h + h' sums to the same residual; the o^3 v tensors are summed in Zmbij
         self.tcc('ma,mbij->ijab', Operand.of('ma', t1), Operand.of('mbij', Zmbij), r, alpha=-1.0)
         # rings
         self.tcc('imae,mbej->ijab', Operand('imae', (t2, 'imae'), Y=(t2, 'imea'), b=-1.0),
@@ -263,15 +284,7 @@ class MixedResidual:
         self.tcc('imae,mbej->ijab', Operand.of('imae', t2),
                  Operand('mbej', (Wmbej, 'mbej'), Y=(Wmbje, 'mbje'), b=1.0), r)
         self.tcc('mjae,mbie->ijab', Operand.of('mjae', t2), Operand.of('mbie', Wmbje), r)
-        # - t_ie t_ma <mb|ej> - t_ie t_mb <ma|je>, two O(o^3 v^2) steps each
-        Y1 = torch.empty((no, no, nv, no), dtype=torch.float64, device=t2.device)
-        self.tcc('ie,mbej->imbj', Operand.of('ie', t1), self.eri('ovvo', 'mbej'), Y1, beta=0.0)
-        self.tcc('ma,imbj->ijab', Operand.of('ma', t1), Operand.of('imbj', Y1), r, alpha=-1.0)
-        Y2 = torch.empty((no, no, nv, no), dtype=torch.float64, device=t2.device)
-        self.tcc('ie,maje->imaj', Operand.of('ie', t1), self.eri('ovov', 'maje'), Y2, beta=0.0)
-        self.tcc('mb,imaj->ijab', Operand.of('mb', t1), Operand.of('imaj', Y2), r, alpha=-1.0)
         self.tcc('ie,abej->ijab', Operand.of('ie', t1), self.eri('vvvo', 'abej'), r)
-        self.tcc('ma,mbij->ijab', Operand.of('ma', t1), self.eri('ovoo', 'mbij'), r, alpha=-1.0)
         return r
 
     def residuals(self, F, t1, t2):

@@ -69,6 +69,67 @@ def test_permuted_operands_and_output(cuda):
     assert frob(r, ref) < TOL[FMT_BF16X3]
 
 
+def _pack_inputs(cuda):
+    """FP64 values across the cases the FP32 rounding of the pack meets: random magnitudes,
+    exact FP32 ties (both parities), signed zeros, FP32's extremes and FP64 values beyond
+    them (which round to zero or infinity)."""
+    g = torch.Generator(device=cuda).manual_seed(11)
+    v = torch.randn(37, 200, generator=g, device=cuda, dtype=torch.float64)
+    v = v * torch.exp2(torch.randint(-60, 60, (37, 200), generator=g, device=cuda).double())
+    ties = []
+    for m in (1, 2, 3, 0x7fffff, 0x400000):              # FP32 mantissas, odd and even
+        base = (1.0 + m * 2.0 ** -23)
+        ties += [base + 2.0 ** -24, -(base + 2.0 ** -24), base + 2.0 ** -24 + 2.0 ** -40,
+                 base + 2.0 ** -24 - 2.0 ** -40]
+    edge = ties + [0.0, -0.0, 1.0, -1.0, 3.4028234663852886e38, 1.1754943508222875e-38,
+                   3.4028235677973366e38, 1e-300, -1e300]
+    v[0, :len(edge)] = torch.tensor(edge, dtype=torch.float64, device=cuda)
+    return v
+
+
+@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3])
+def test_pack_rounding_bit_exact(cuda, fmt):
+    """Packed pieces equal FP64 -> FP32 (round to nearest even) -> BF16 pieces, bit for bit:
+    hi = bf16(f), lo = bf16(f - hi) with f the FP32 rounding of the value (zero below
+    FP32's normal range, infinity above it)."""
+    from pycc_gb300.tc import pack
+    v = _pack_inputs(cuda)
+    P = pack(Operand.of("rk", v), "r", "k", fmt)
+    torch.cuda.synchronize()
+    f = v.float()
+    f = torch.where(f.abs() < 2.0 ** -126, f * 0.0, f)        # signed zero
+    hi = f.bfloat16()
+    K = v.shape[1]
+    assert torch.equal(P.hi[:, :K].view(torch.int16), hi.view(torch.int16))
+    assert torch.all(P.hi[:, K:].float() == 0)
+    if fmt == FMT_BF16X3:
+        lo = torch.where(torch.isinf(f), torch.full_like(f, float("nan")), f - hi.float())
+        lo = lo.bfloat16()
+        fin = torch.isfinite(f)
+        assert torch.equal(P.lo[:, :K][fin].view(torch.int16), lo[fin].view(torch.int16))
+
+
+def test_pack_combination(cuda):
+    """a*X + b*Y + c*P*Q with permuted sources, K padding and a row table, against FP64
+    within the FP32 rounding of the operands."""
+    from pycc_gb300.tc import pack
+    g = torch.Generator(device=cuda).manual_seed(12)
+    X = torch.randn(7, 9, 70, generator=g, device=cuda, dtype=torch.float64)
+    Y = torch.randn(9, 7, 70, generator=g, device=cuda, dtype=torch.float64)
+    Pm = torch.randn(7, 70, generator=g, device=cuda, dtype=torch.float64)
+    Q = torch.randn(9, generator=g, device=cuda, dtype=torch.float64)
+    op = Operand("ijk", (X, "ijk"), a=2.0, Y=(Y, "jik"), b=-0.5, P=(Pm, "ik"), Q=(Q, "j"), c=0.25)
+    P = pack(op, "ij", "k", FMT_BF16X3)
+    torch.cuda.synchronize()
+    parts = (2.0 * X, -0.5 * Y.transpose(0, 1), 0.25 * Pm[:, None, :] * Q[None, :, None])
+    ref = sum(parts).reshape(63, 70)
+    scale = sum(q.abs() for q in parts).reshape(63, 70)
+    got = P.hi[:, :70].double() + P.lo[:, :70].double()
+    # split error 2^-17 of the value, FP32 combination 2^-24 of each operand (a few roundings)
+    assert torch.all((got - ref).abs() <= 2.0 ** -16 * ref.abs() + 2.0 ** -21 * scale)
+    assert torch.all(P.hi[:, 70:].float() == 0) and torch.all(P.lo[:, 70:].float() == 0)
+
+
 def test_split_k_small_output(cuda):
     g = torch.Generator(device=cuda).manual_seed(2)
     A = torch.randn(40, 60000, generator=g, device=cuda, dtype=torch.float64)
