@@ -112,6 +112,16 @@ int pcg_diis_error_f64(const double* x, const double* old, double* e, const doub
                        int k, long long n, double* work, long long work_len, double* out,
                        void* stream);
 
+/* pcg_diis_error_f64 with FP32 error vectors, for the mixed-precision solver: e = x - old
+ * taken in FP64 and rounded once to FP32; overlaps from FP32 products of four consecutive
+ * elements, accumulated in FP64.  x, old, e and ys[j] 16-byte aligned.  The reference's
+ * helper_diis keeps its error vectors in the amplitudes' own precision
+ * (pycc/utils.py:284-295, :330-339); this is its storage at the precision of the
+ * tensor-core residual. */
+int pcg_diis_error_f32(const double* x, const double* old, float* e, const float* const* ys,
+                       int k, long long n, double* work, long long work_len, double* out,
+                       void* stream);
+
 /* out = sum_j c[j]*xs[j], 1 <= k <= 16 (xs, c on the host; out must not alias an input).
  * DIIS extrapolation, helper_diis.extrapolate (pycc/utils.py:351-355) */
 int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n, double* out,

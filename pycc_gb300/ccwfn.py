@@ -380,7 +380,10 @@ class CCwfn:
         self.energies = [ecc]
         self.iter_times = []
         self._last_rms = float('inf')
-        return DIIS(self._amps, max_diis, self.stream)
+        # the mixed solver's residual carries ~2^-17 relative rounding: FP32 error vectors
+        # hold its updates to better than that, at half the bytes
+        edt = torch.float32 if self.precision == 'MIXED' else torch.float64
+        return DIIS(self._amps, max_diis, self.stream, error_dtype=edt)
 
     def iterate(self, diis, niter, start_diis=1, extrapolate=True):
         """One Jacobi + DIIS iteration (ccwfn.py:270-319); returns (ecc, rms).

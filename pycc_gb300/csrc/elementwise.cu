@@ -200,7 +200,9 @@ __global__ void dots_kernel(const double* __restrict__ x, VecList ys, int k, lon
     for (int j = 0; j < kMaxVec; ++j)
       if (j < k) acc[j] += xv * ys.p[j][idx];
   }
-  for (int j = 0; j < k; ++j) {
+#pragma unroll
+  for (int j = 0; j < kMaxVec; ++j) {  // constant indices keep acc in registers
+    if (j >= k) break;
     double v = block_sum(acc[j]);
     if (threadIdx.x == 0) part[(long long)j * gridDim.x + blockIdx.x] = v;
     __syncthreads();
@@ -223,7 +225,62 @@ __global__ void diis_error_kernel(const double* __restrict__ x, const double* __
       if (j < k - 1) acc[j] += ev * ys.p[j][idx];
     acc[kMaxVec - 1] += ev * ev;
   }
-  for (int j = 0; j < k; ++j) {
+  // constant indices (unrolled) keep acc in registers; j < k is uniform over the block
+#pragma unroll
+  for (int j = 0; j < kMaxVec; ++j) {
+    if (j >= k) break;
+    double v = block_sum(j == k - 1 ? acc[kMaxVec - 1] : acc[j]);
+    if (threadIdx.x == 0) part[(long long)j * gridDim.x + blockIdx.x] = v;
+    __syncthreads();
+  }
+}
+
+struct VecListF {
+  const float* p[kMaxVec];
+};
+
+// Mixed-precision DIIS error pass: e = FP32(x - old) (the difference taken in FP64 and
+// rounded once, in integer arithmetic) and its overlaps with the k-1 stored FP32 error
+// vectors and itself.  Four consecutive elements per step: their FP32 products are summed
+// in FP32 and each step's sum is accumulated in FP64, so a vector of n elements costs
+// n + k n / 4 FP64 additions instead of the k n of the FP64 pass.
+__global__ void diis_error_f32_kernel(const double* __restrict__ x,
+                                      const double* __restrict__ old, float* __restrict__ e,
+                                      VecListF ys, int k, long long n,
+                                      double* __restrict__ part) {
+  double acc[kMaxVec];
+#pragma unroll
+  for (int j = 0; j < kMaxVec; ++j) acc[j] = 0.0;
+  const long long n4 = n >> 2;
+  const double2* x2 = reinterpret_cast<const double2*>(x);
+  const double2* o2 = reinterpret_cast<const double2*>(old);
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n4;
+       q += (long long)gridDim.x * blockDim.x) {
+    const double2 xa = x2[2 * q], xb = x2[2 * q + 1], oa = o2[2 * q], ob = o2[2 * q + 1];
+    const float4 ev = make_float4(f64_to_f32(xa.x - oa.x), f64_to_f32(xa.y - oa.y),
+                                  f64_to_f32(xb.x - ob.x), f64_to_f32(xb.y - ob.y));
+    reinterpret_cast<float4*>(e)[q] = ev;
+#pragma unroll
+    for (int j = 0; j < kMaxVec - 1; ++j)
+      if (j < k - 1) {
+        const float4 y = reinterpret_cast<const float4*>(ys.p[j])[q];
+        acc[j] += f32_to_f64(ev.x * y.x + ev.y * y.y + ev.z * y.z + ev.w * y.w);
+      }
+    acc[kMaxVec - 1] += f32_to_f64(ev.x * ev.x + ev.y * ev.y + ev.z * ev.z + ev.w * ev.w);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {  // the last n mod 4 elements
+    const long long i = (n4 << 2) + threadIdx.x;
+    const float v = f64_to_f32(x[i] - old[i]);
+    e[i] = v;
+#pragma unroll
+    for (int j = 0; j < kMaxVec - 1; ++j)
+      if (j < k - 1) acc[j] += f32_to_f64(v * ys.p[j][i]);
+    acc[kMaxVec - 1] += f32_to_f64(v * v);
+  }
+  // constant indices (unrolled) keep acc in registers; j < k is uniform over the block
+#pragma unroll
+  for (int j = 0; j < kMaxVec; ++j) {
+    if (j >= k) break;
     double v = block_sum(j == k - 1 ? acc[kMaxVec - 1] : acc[j]);
     if (threadIdx.x == 0) part[(long long)j * gridDim.x + blockIdx.x] = v;
     __syncthreads();
@@ -393,6 +450,44 @@ extern "C" int pcg_diis_error_f64(const double* x, const double* old, double* e,
   PCG_CHECK_LAUNCH("pcg_diis_error_f64/partials");
   finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, k, out);
   PCG_CHECK_LAUNCH("pcg_diis_error_f64");
+  return 0;
+}
+
+// FP32 error storage for the mixed-precision solver (see diis_error_f32_kernel); the
+// pointers are 16-byte aligned (vector loads of four elements).
+extern "C" int pcg_diis_error_f32(const double* x, const double* old, float* e,
+                                  const float* const* ys, int k, long long n, double* work,
+                                  long long work_len, double* out, void* stream) {
+  if (k < 1 || k > kMaxVec) {
+    set_error("pcg_diis_error_f32: k=%d outside [1, %d]", k, kMaxVec);
+    return -1;
+  }
+  if (!x || !old || !e || !out || n < 0) {
+    set_error("pcg_diis_error_f32: bad arguments");
+    return -1;
+  }
+  auto al16 = [](const void* q) { return ((uintptr_t)q & 15u) == 0; };
+  bool ok = al16(x) && al16(old) && al16(e);
+  VecListF v{};
+  for (int j = 0; j + 1 < k; ++j) {
+    if (!ys || !ys[j]) {
+      set_error("pcg_diis_error_f32: null stored error vector %d", j);
+      return -1;
+    }
+    v.p[j] = ys[j];
+    ok = ok && al16(ys[j]);
+  }
+  if (!ok) {
+    set_error("pcg_diis_error_f32: vectors must be 16-byte aligned");
+    return -1;
+  }
+  if (!check_work(work_len, (long long)k * RED_BLOCKS, "pcg_diis_error_f32")) return -1;
+  cudaStream_t st = (cudaStream_t)stream;
+  int nb = std::min(ew_blocks(std::max(n / 4, 1LL)), RED_BLOCKS);
+  diis_error_f32_kernel<<<nb, EW_THREADS, 0, st>>>(x, old, e, v, k, n, work);
+  PCG_CHECK_LAUNCH("pcg_diis_error_f32/partials");
+  finish_sum_kernel<<<1, EW_THREADS, 0, st>>>(work, nb, k, out);
+  PCG_CHECK_LAUNCH("pcg_diis_error_f32");
   return 0;
 }
 

@@ -485,9 +485,9 @@ __device__ __forceinline__ V pack_ld(const double* q) {
   else return f64_to_f32(*q);
 }
 
-template <typename V>
+template <typename V, bool KF>
 __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t, long long r0,
-                                               long long k0, int kfast) {
+                                               long long k0) {
   const int tid = threadIdx.x;
   if (tid < TR) {
     long long o[4] = {0, 0, 0, 0};
@@ -506,45 +506,58 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
   }
   __syncthreads();
   const V a = (V)p.a, b = (V)p.b, c = (V)p.c;
-  // all of a thread's gathers are issued before the first shared-memory store
-  constexpr int PER = TR * TK / PACK_THREADS;
+  // Each thread keeps one index of the unit-stride side fixed (a K column when KF, a row
+  // otherwise), so consecutive threads read consecutive addresses, and walks the other
+  // side; the fixed side's offsets and bound are read once.  All of a thread's gathers
+  // are issued before its first shared-memory store.
+  constexpr int NF = KF ? TK : TR;
+  constexpr int STEP = PACK_THREADS / NF;
+  constexpr int PER = (KF ? TR : TK) / STEP;
+  const int fx = tid % NF, w0 = tid / NF;
+  const bool fx_ok = KF ? (k0 + fx < p.K) : (r0 + fx < p.R);
+  const long long wlim = KF ? (p.R - r0) : (p.K - k0);
+  long long f[4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) f[s] = KF ? t.kof[s][fx] : t.rof[s][fx];
   V vals[PER];
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
-    const int e = tid + u * PACK_THREADS;
-    int rr, kk;
-    if (kfast) { rr = e / TK; kk = e % TK; } else { kk = e / TR; rr = e % TR; }
+    const int wv = w0 + u * STEP;
     V v = 0;
-    if (r0 + rr < p.R && k0 + kk < p.K) {
-      if (p.X) v = a * pack_ld<V>(p.X + t.rof[0][rr] + t.kof[0][kk]);
-      if (p.Y) v += b * pack_ld<V>(p.Y + t.rof[1][rr] + t.kof[1][kk]);
-      if (p.P)
-        v += c * pack_ld<V>(p.P + t.rof[2][rr] + t.kof[2][kk]) *
-             pack_ld<V>(p.Q + t.rof[3][rr] + t.kof[3][kk]);
+    if (fx_ok && wv < wlim) {
+      const long long w[4] = {KF ? t.rof[0][wv] : t.kof[0][wv], KF ? t.rof[1][wv] : t.kof[1][wv],
+                              KF ? t.rof[2][wv] : t.kof[2][wv], KF ? t.rof[3][wv] : t.kof[3][wv]};
+      if (p.X) v = a * pack_ld<V>(p.X + f[0] + w[0]);
+      if (p.Y) v += b * pack_ld<V>(p.Y + f[1] + w[1]);
+      if (p.P) v += c * pack_ld<V>(p.P + f[2] + w[2]) * pack_ld<V>(p.Q + f[3] + w[3]);
     }
     vals[u] = v;
   }
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
-    const int e = tid + u * PACK_THREADS;
-    int rr, kk;
-    if (kfast) { rr = e / TK; kk = e % TK; } else { kk = e / TR; rr = e % TR; }
-    t.v[rr][kk] = vals[u];
+    const int wv = w0 + u * STEP;
+    if (KF)
+      t.v[wv][fx] = vals[u];
+    else
+      t.v[fx][wv] = vals[u];
   }
   __syncthreads();
 }
 
 // BF16 / split-BF16x3 from an FP32 tile: two adjacent K entries per thread, written as one
 // bf16x2 word (K offsets are even: Kp and k0 are multiples of 64).
-__global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs p, int kfast) {
+template <bool KF>
+__global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs p) {
   __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
-  pack_tile_load(p, t, r0, k0, kfast);
+  pack_tile_load<float, KF>(p, t, r0, k0);
   __nv_bfloat162* hi = reinterpret_cast<__nv_bfloat162*>(p.hi);
   __nv_bfloat162* lo = reinterpret_cast<__nv_bfloat162*>(p.lo);
-  for (int e = threadIdx.x; e < TR * TK / 2; e += PACK_THREADS) {
-    const int rr = e / (TK / 2), kk = 2 * (e % (TK / 2));
-    if (r0 + rr >= p.R) continue;
+  static_assert(TK == 64, "a warp writes one 64-entry row of the tile");
+  const int kk = 2 * (threadIdx.x & 31);
+#pragma unroll 4
+  for (int rr = threadIdx.x >> 5; rr < TR; rr += PACK_THREADS / 32) {
+    if (r0 + rr >= p.R) break;
     const long long at = ((r0 + rr) * p.Kp + k0 + kk) >> 1;
     const float v0 = t.v[rr][kk], v1 = t.v[rr][kk + 1];
     const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
@@ -554,10 +567,11 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs 
 }
 
 // Split-BF16x6 (hi, mid, lo) from an FP64 tile.
-__global__ void __launch_bounds__(PACK_THREADS) pack_bf16x6_kernel(const PackArgs p, int kfast) {
+template <bool KF>
+__global__ void __launch_bounds__(PACK_THREADS) pack_bf16x6_kernel(const PackArgs p) {
   __shared__ PackTile<double> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
-  pack_tile_load(p, t, r0, k0, kfast);
+  pack_tile_load<double, KF>(p, t, r0, k0);
   __nv_bfloat16* hi = reinterpret_cast<__nv_bfloat16*>(p.hi);
   __nv_bfloat16* mid = reinterpret_cast<__nv_bfloat16*>(p.mid);
   __nv_bfloat16* lo = reinterpret_cast<__nv_bfloat16*>(p.lo);
@@ -578,11 +592,12 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_bf16x6_kernel(const PackArg
 
 // FP8 pass 1: per-row max |v| into rowmax (float bits, zero-initialised; |v| >= 0 so the
 // unsigned order of the bits is the float order).
-__global__ void __launch_bounds__(PACK_THREADS) pack_fp8_max_kernel(const PackArgs p, int kfast,
+template <bool KF>
+__global__ void __launch_bounds__(PACK_THREADS) pack_fp8_max_kernel(const PackArgs p,
                                                                     unsigned* rowmax) {
   __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
-  pack_tile_load(p, t, r0, k0, kfast);
+  pack_tile_load<float, KF>(p, t, r0, k0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int rr = warp; rr < TR; rr += PACK_THREADS / 32) {
     float m = fmaxf(fabsf(t.v[rr][lane]), fabsf(t.v[rr][lane + 32]));
@@ -606,11 +621,12 @@ __global__ void pack_fp8_scale_kernel(long long R, unsigned* rowmax_scale) {
 }
 
 // FP8 pass 3: quantise with the row's scale (a power of two, so the FP32 product is exact).
-__global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p, int kfast,
+template <bool KF>
+__global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p,
                                                                 const float* scale) {
   __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
-  pack_tile_load(p, t, r0, k0, kfast);
+  pack_tile_load<float, KF>(p, t, r0, k0);
   __nv_fp8_e4m3* dst = reinterpret_cast<__nv_fp8_e4m3*>(p.hi);
   for (int e = threadIdx.x; e < TR * TK; e += PACK_THREADS) {
     const int rr = e / TK, kk = e % TK;
@@ -807,15 +823,27 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   if (fmt == kFP8) {
     unsigned* mx = reinterpret_cast<unsigned*>(row_scale);
     cudaMemsetAsync(mx, 0, sizeof(float) * p.R, st);
-    pack_fp8_max_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, mx);
+    if (kfast)
+      pack_fp8_max_kernel<true><<<grid, PACK_THREADS, 0, st>>>(p, mx);
+    else
+      pack_fp8_max_kernel<false><<<grid, PACK_THREADS, 0, st>>>(p, mx);
     PCG_CHECK_LAUNCH("pcg_pack_operand/max");
     pack_fp8_scale_kernel<<<(unsigned)std::min<long long>((p.R + 255) / 256, 4096), 256, 0, st>>>(p.R, mx);
     PCG_CHECK_LAUNCH("pcg_pack_operand/scale");
-    pack_fp8_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast, row_scale);
+    if (kfast)
+      pack_fp8_kernel<true><<<grid, PACK_THREADS, 0, st>>>(p, row_scale);
+    else
+      pack_fp8_kernel<false><<<grid, PACK_THREADS, 0, st>>>(p, row_scale);
   } else if (fmt == kBF16x6) {
-    pack_bf16x6_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast);
+    if (kfast)
+      pack_bf16x6_kernel<true><<<grid, PACK_THREADS, 0, st>>>(p);
+    else
+      pack_bf16x6_kernel<false><<<grid, PACK_THREADS, 0, st>>>(p);
   } else {
-    pack_bf16_kernel<<<grid, PACK_THREADS, 0, st>>>(p, kfast);
+    if (kfast)
+      pack_bf16_kernel<true><<<grid, PACK_THREADS, 0, st>>>(p);
+    else
+      pack_bf16_kernel<false><<<grid, PACK_THREADS, 0, st>>>(p);
   }
   PCG_CHECK_LAUNCH("pcg_pack_operand");
   return 0;

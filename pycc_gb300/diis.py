@@ -6,6 +6,10 @@ on the GPU, computed once per new vector against every stored one (the reference
 the full matrix each call; the values are the same); the bordered (k+1)^2 Pulay system is
 scaled by its largest |B| entry (``utils.py:341``) and solved in FP64; the new amplitudes
 ``sum_i c_i t_i`` are one fused linear-combination pass.
+
+With ``error_dtype=torch.float32`` (the mixed-precision solver) the error vectors are kept
+in FP32: each is the FP64 difference rounded once, and the overlaps come from FP32 products
+accumulated in FP64.  The amplitudes and their extrapolation stay FP64.
 """
 from __future__ import annotations
 
@@ -20,10 +24,14 @@ WORK_LEN = 16 * 1024
 
 
 class DIIS:
-    def __init__(self, amps: torch.Tensor, max_diis: int, stream=None):
+    def __init__(self, amps: torch.Tensor, max_diis: int, stream=None,
+                 error_dtype=torch.float64):
         """``amps`` is the flat FP64 ``[t1 | t2]`` vector the solver iterates."""
+        if error_dtype not in (torch.float64, torch.float32):
+            raise ValueError("DIIS: error vectors are float64 or float32")
         self.max_diis = int(max_diis)
         self.stream = stream
+        self.error_dtype = error_dtype
         self.old = amps.clone()
         self.vals = [amps.clone()]
         self.errors = []
@@ -34,11 +42,12 @@ class DIIS:
     def add_error_vector(self, amps: torch.Tensor):
         self.vals.append(amps.clone())
         k = len(self.errors) + 1
-        e = torch.empty_like(amps)
+        e = torch.empty(amps.shape, dtype=self.error_dtype, device=amps.device)
         # e = amps - old, written once, and its overlaps with every stored error vector
         # (itself included) in the same pass
         ptrs = (C.c_void_p * k)(*([x.data_ptr() for x in self.errors] + [0]))
-        _lib.call("pcg_diis_error_f64", amps.data_ptr(), self.old.data_ptr(), e.data_ptr(), ptrs,
+        fn = "pcg_diis_error_f64" if self.error_dtype == torch.float64 else "pcg_diis_error_f32"
+        _lib.call(fn, amps.data_ptr(), self.old.data_ptr(), e.data_ptr(), ptrs,
                   k, e.numel(), self.work.data_ptr(), self.work.numel(), self.dots.data_ptr(),
                   _lib.stream_handle(self.stream))
         self.errors.append(e)
