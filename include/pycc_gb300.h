@@ -183,7 +183,7 @@ int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, 
 
 /* Grouped segmented BF16 GEMM with FP32 output, the connected-triples builder of the (T)
  * correction (t3c_ijk, pycc/cctriples.py:56-67, for a batch of triples).  Group g computes
- *   C[out_g + m*ldc + n] = sum_s A[amap_gs][arow_gs + m, :] . B[bmap_gs][brow_gs + n, :]
+ *   C[out_g + m*ldm + n*ldn] = sum_s A[amap_gs][arow_gs + m, :] . B[bmap_gs][brow_gs + n, :]
  * for m < M, n < N over its nseg <= 4 K segments (nkb_gs K blocks of 64).  a_ptr / b_ptr:
  * host arrays of up to four BF16 K-major operand matrices (a_rows[q] rows of a_ld[q]
  * elements).  groups: device array of ngroups records of pcg_tc_group_desc_size() bytes:
@@ -191,8 +191,8 @@ int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, 
 int pcg_tc_grouped_gemm(int na, const void* const* a_ptr, const long long* a_rows,
                         const long long* a_ld, int nb, const void* const* b_ptr,
                         const long long* b_rows, const long long* b_ld, const void* groups,
-                        int ngroups, long long M, long long N, float* C, long long ldc,
-                        int* status, void* stream);
+                        int ngroups, long long M, long long N, float* C, long long ldm,
+                        long long ldn, int* status, void* stream);
 int pcg_tc_group_desc_size(void);
 
 #ifdef __cplusplus

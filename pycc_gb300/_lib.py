@@ -46,7 +46,8 @@ SIGNATURES = {
                                      _i64, _i64, _p, _p]),
     "pcg_reduce_sum_f64": (C.c_int, [_p, _i64, _p, _p]),
     "pcg_tc_grouped_gemm": (C.c_int, [C.c_int, C.POINTER(_p), _pi64, _pi64, C.c_int, C.POINTER(_p),
-                                      _pi64, _pi64, _p, C.c_int, _i64, _i64, _p, _i64, _p, _p]),
+                                      _pi64, _pi64, _p, C.c_int, _i64, _i64, _p, _i64, _i64, _p,
+                                      _p]),
     "pcg_tc_group_desc_size": (C.c_int, []),
     "pcg_pack_operand": (C.c_int, [C.c_int, C.c_int, _pi64, _pi64, C.c_int, _pi64, _pi64, _i64,
                                    _d, _p, _d, _p, _d, _p, _p, _p, _p, _p, _p, _p, _i64, _p]),

@@ -903,16 +903,18 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.col_map = col_map;
   a.col_scale = col_scale;
   a.status = status;
-  // tile width: least padded work, weighting each tile by its fixed A-operand share
+  // Tile width: the least SM time, counting whole waves of the persistent grid (a launch
+  // with fewer tiles than SMs is split along K instead) and weighting each tile by its
+  // columns plus its fixed A-operand share.
   static const int kBN[] = {64, 96, 128, 160, 192, 224, 256};
-  static const int kBNfused[] = {64, 128, 256};
   const bool fused = (fmt == kBF16x3F);
+  const long long sms_all = num_sms();
   int BN = 64;
   long long best = -1;
   for (int bn : kBN) {
-    if (fused && bn != kBNfused[0] && bn != kBNfused[1] && bn != kBNfused[2]) continue;
-    const long long tiles_n = (N + bn - 1) / bn;
-    const long long cost = tiles_n * (bn + 48);
+    const long long tiles = ((M + BM - 1) / BM) * ((N + bn - 1) / bn);
+    const long long slots = tiles >= sms_all ? (tiles + sms_all - 1) / sms_all * sms_all : tiles;
+    const long long cost = slots * (bn + 48);
     if (best < 0 || cost < best || (cost == best && bn > BN)) {
       best = cost;
       BN = bn;
@@ -958,7 +960,11 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   if (fused) {
     switch (BN) {
       case 64: return launch<64, 2>(maps, a, st);
+      case 96: return launch<96, 2>(maps, a, st);
       case 128: return launch<128, 2>(maps, a, st);
+      case 160: return launch<160, 2>(maps, a, st);
+      case 192: return launch<192, 2>(maps, a, st);
+      case 224: return launch<224, 2>(maps, a, st);
       default: return launch<256, 2>(maps, a, st);
     }
   }

@@ -4,11 +4,14 @@
 // (m < M, n < N) where each group has up to four K segments; segment s reads K-major BF16
 // rows from one of four A operand matrices and one of four B operand matrices (TMA maps),
 // starting at a per-group row.  All segments of a group accumulate in one TMEM tile, so
-// the output (FP32, C[out_g + m*ldc + n]) is written once.  For the (T) correction a group is
-// one (triple, orientation) and its segments are the four t3 terms of that orientation.
+// the output (FP32, C[out_g + m*ldm + n*ldn]) is written once.  For the (T) correction a group
+// is one (triple, orientation) and its segments are the four t3 terms of that orientation;
+// its partial is stored column-major (ldm = 1), so that the 32 rows a warp drains from
+// TMEM (one per lane) are 32 consecutive floats.
 //
-// Persistent and warp-specialised like tc_gemm_kernel: warp 0 TMA, warp 1 MMA, warps 2-5
-// epilogue, two TMEM accumulators; every mbarrier wait is bounded.
+// Persistent and warp-specialised like tc_gemm_kernel: warp 0 TMA, warp 1 MMA, warps 2-9
+// epilogue (two per TMEM lane quarter, one per column half), two TMEM accumulators; every
+// mbarrier wait is bounded.
 #include "tc_common.cuh"
 #include <algorithm>
 
@@ -28,10 +31,13 @@ struct GMaps {
   CUtensorMap b[4];
 };
 
+constexpr int GROUPED_EPI_WARPS = 8;
+constexpr int GROUPED_THREADS = 64 + 32 * GROUPED_EPI_WARPS;
+
 struct GArgs {
   const GroupDesc* groups;
   int ngroups;
-  long long M, N, ldc;
+  long long M, N, ldm, ldn;
   long long mt, nt;
   float* C;
   int* status;
@@ -50,7 +56,7 @@ struct GSmem {
 };
 
 template <int BN>
-__global__ void __launch_bounds__(NT, 1)
+__global__ void __launch_bounds__(GROUPED_THREADS, 1)
     tc_grouped_kernel(const __grid_constant__ GMaps maps, const GArgs p) {
   using L = GSmem<BN>;
   constexpr int S = L::STAGES;
@@ -80,7 +86,7 @@ __global__ void __launch_bounds__(NT, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&tfull[b], 1);
-      mbar_init(&tempty[b], EPI_THREADS / 32);
+      mbar_init(&tempty[b], GROUPED_EPI_WARPS);
     }
     mbar_init(mdone, 1);
     *abort_flag = 0;
@@ -174,7 +180,10 @@ __global__ void __launch_bounds__(NT, 1)
     }
     __syncwarp();
   } else {
-    const int q = warp & 3;
+    const int q = warp & 3;         // TMEM lane quarter
+    const int h = (warp - 2) >> 2;  // column half: alternate 32-column blocks, last odd
+                                    // block split 16 / 16 (loads start at their width)
+    constexpr int NFULL = BN / 64;
     int ui = 0;
     for (long long u = blockIdx.x; u < nunits; u += gridDim.x, ++ui) {
       const GroupDesc& g = p.groups[u / per];
@@ -193,15 +202,27 @@ __global__ void __launch_bounds__(NT, 1)
       if (!__shfl_sync(0xffffffffu, okw, 0)) break;
       tc_fence_after();
       const long long row = m0 + q * 32 + lane;
-      float* crow = p.C + g.out + row * p.ldc;
+      const bool row_ok = row < p.M;
+      float* crow = p.C + g.out + row * p.ldm;
+      const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
-      for (int cc = 0; cc < BN; cc += 32) {
+      for (int fb = 0; fb < NFULL; ++fb) {
+        const int c0 = 32 * (2 * fb + h);
         uint32_t v[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN + cc), v);
-        if (row >= p.M) continue;
+        tmem_ld32(tb + c0, v);
+        if (row_ok)
 #pragma unroll
-        for (int j = 0; j < 32; ++j)
-          if (n0 + cc + j < p.N) crow[n0 + cc + j] = __uint_as_float(v[j]);
+          for (int j = 0; j < 32; ++j)
+            if (n0 + c0 + j < p.N) crow[(n0 + c0 + j) * p.ldn] = __uint_as_float(v[j]);
+      }
+      if constexpr (BN % 64 != 0) {
+        const int c0 = BN - 32 + 16 * h;
+        uint32_t v[16];
+        tmem_ld16(tb + c0, v);
+        if (row_ok)
+#pragma unroll
+          for (int j = 0; j < 16; ++j)
+            if (n0 + c0 + j < p.N) crow[(n0 + c0 + j) * p.ldn] = __uint_as_float(v[j]);
       }
       tc_fence_before();
       __syncwarp();
@@ -228,7 +249,7 @@ int glaunch(const GMaps& maps, GArgs a, cudaStream_t st) {
   a.nt = (a.N + BN - 1) / BN;
   const long long units = a.mt * a.nt * a.ngroups;
   const long long grid = std::min<long long>(units, num_sms());
-  tc_grouped_kernel<BN><<<(unsigned)grid, NT, smem, st>>>(maps, a);
+  tc_grouped_kernel<BN><<<(unsigned)grid, GROUPED_THREADS, smem, st>>>(maps, a);
   PCG_CHECK_LAUNCH("pcg_tc_grouped_gemm");
   return 0;
 }
@@ -242,14 +263,16 @@ using namespace pcg::tc;
 // Grouped segmented BF16 GEMM, FP32 output (see the top of this file).  a_ptr / b_ptr: up
 // to four BF16 operand matrices each ([a_rows[q]][a_ld[q]] K-major, 16-byte aligned rows,
 // K a multiple of 64); groups: device array of ngroups GroupDesc records (nseg, amap[4],
-// arow[4], bmap[4], brow[4], nkb[4], out) as laid out in this file.
+// arow[4], bmap[4], brow[4], nkb[4], out) as laid out in this file; element (m, n) of group
+// g goes to C[out_g + m*ldm + n*ldn].
 extern "C" int pcg_tc_grouped_gemm(int na, const void* const* a_ptr, const long long* a_rows,
                                    const long long* a_ld, int nb, const void* const* b_ptr,
                                    const long long* b_rows, const long long* b_ld,
                                    const void* groups, int ngroups, long long M, long long N,
-                                   float* C, long long ldc, int* status, void* stream) {
+                                   float* C, long long ldm, long long ldn, int* status,
+                                   void* stream) {
   if (na < 1 || na > 4 || nb < 1 || nb > 4 || !groups || ngroups < 1 || M < 1 || N < 1 || !C ||
-      !status || ldc < N) {
+      !status || ldm < 1 || ldn < 1 || M > 0x7fffffffLL || N > 0x7fffffffLL) {
     set_error("pcg_tc_grouped_gemm: bad arguments");
     return -1;
   }
@@ -272,7 +295,8 @@ extern "C" int pcg_tc_grouped_gemm(int na, const void* const* a_ptr, const long 
   a.ngroups = ngroups;
   a.M = M;
   a.N = N;
-  a.ldc = ldc;
+  a.ldm = ldm;
+  a.ldn = ldn;
   a.mt = (M + BM - 1) / BM;
   a.C = C;
   a.status = status;

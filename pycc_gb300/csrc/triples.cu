@@ -2,11 +2,12 @@
 //
 // The connected triples W[a,b,c] of one triple arrive as three partial tensors, one per
 // orientation of the twelve t3 terms (the terms of an orientation share their output
-// layout, so each partial is written once by a single contraction):
-//   P1[a][b][c]  (terms t2_kj <bc..> etc. with rows (a,b), column c)
-//   P2[a][c][b]  (rows (a,c), column b)
-//   P3[b][c][a]  (rows (b,c), column a)
-//   W[a,b,c] = P1[a,b,c] + P2[a,c,b] + P3[b,c,a]
+// layout, so each partial is written once by a single contraction).  Each is the output of
+// a GEMM with rows (two virtual indices) and one column index, stored column-major:
+//   orientation 1: rows (a,b), column c  ->  P1[c][a][b]
+//   orientation 2: rows (a,c), column b  ->  P2[b][a][c]
+//   orientation 3: rows (b,c), column a  ->  P3[a][b][c]
+//   W[a,b,c] = P1[c][a][b] + P2[b][a][c] + P3[a][b][c]
 // The Lee-Rendell energy of the reference (pycc/cctriples.py:177-240) is then evaluated
 // for a >= b >= c with the same weights; one block per (triple, a), one FP64 partial per
 // block (deterministic reduction by pcg_reduce_sum_f64).
@@ -39,7 +40,7 @@ template <typename T>
 __device__ __forceinline__ T wval(const TripArgs<T>& p, const T* P1, const T* P2, const T* P3,
                                   long long x, long long y, long long z) {
   const long long v = p.nv;
-  return P1[(x * v + y) * v + z] + P2[(x * v + z) * v + y] + P3[(y * v + z) * v + x];
+  return P1[(z * v + x) * v + y] + P2[(y * v + x) * v + z] + P3[(x * v + y) * v + z];
 }
 
 // disconnected triples (pycc/cctriples.py:133-140) at (x, y, z), in the arithmetic type T

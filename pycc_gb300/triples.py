@@ -7,7 +7,9 @@ built as three partial tensors, one per output orientation of the twelve t3 term
 * orientation 2, P2[a,c,b]: t2_jk <ca|ei>, t2_ji <ac|ek>, -t2_imac <mb|kj>, -t2_kmca <mb|ij>
 * orientation 3, P3[b,c,a]: t2_ij <bc|ek>, t2_ik <cb|ej>, -t2_kmcb <ma|ji>, -t2_jmbc <ma|ki>
 
-so each partial is written once by one multi-term contraction.  The energy kernel
+so each partial is written once by one multi-term contraction.  A partial is stored with its
+last (column) index slowest, P[z][x][y] for the logical P[x,y,z], the layout in which the
+tensor-core GEMM writes it with coalesced stores.  The energy kernel
 (``csrc/triples.cu``) adds the partials, the disconnected triples (``t3d_ijk``) and the
 Lee-Rendell weights, and accumulates E(T) in FP64.
 
@@ -114,7 +116,7 @@ def t_energy_fp64(w, t1=None, t2=None):
     ijk = torch.tensor(trips, dtype=torch.int32, device=dev)
     for t, (i, j, k) in enumerate(trips):
         for q, (lab, terms) in enumerate(orientation_terms(i, j, k, t2, V, O)):
-            contract_multi(P[q], lab, terms, stream=w.stream)
+            contract_multi(P[q].permute(1, 2, 0), lab, terms, stream=w.stream)
         _energy(False, P[0], P[1], P[2], 0, ijk[t:t + 1], 1, w, t1, t2, part[t:t + 1], w.stream)
     out = torch.zeros((), dtype=torch.float64, device=dev)
     _lib.call("pcg_reduce_sum_f64", part.data_ptr(), part.numel(), out.data_ptr(),

@@ -67,33 +67,38 @@ class TriplesTC:
             raise _lib.EngineError("GroupDesc layout mismatch")
 
     def groups(self, trips):
+        """GroupDesc records of the three orientations of every triple (numpy, vectorised)."""
         no, nv = self.no, self.nv
         v2, v3 = nv * nv, nv ** 3
         kv, ko = self.nkb_v, self.nkb_o
-        g = np.zeros(3 * len(trips), dtype=GROUP_DTYPE)
+        tr = np.asarray(trips, dtype=np.int64).reshape(-1, 3)
+        i, j, k = tr[:, 0], tr[:, 1], tr[:, 2]
+        nt = len(tr)
+        g = np.zeros(3 * nt, dtype=GROUP_DTYPE)
 
         def row_b(x, y):
             return (x * no + y) * nv
 
-        for t, (i, j, k) in enumerate(trips):
-            segs = [
-                [(VT, i, T2P, row_b(k, j), kv), (VN, j, T2P, row_b(k, i), kv),
-                 (TM, i, OB, row_b(j, k), ko), (TMT, j, OB, row_b(i, k), ko)],
-                [(VT, i, T2P, row_b(j, k), kv), (VN, k, T2P, row_b(j, i), kv),
-                 (TM, i, OB, row_b(k, j), ko), (TMT, k, OB, row_b(i, j), ko)],
-                [(VN, k, T2P, row_b(i, j), kv), (VT, j, T2P, row_b(i, k), kv),
-                 (TMT, k, OB, row_b(j, i), ko), (TM, j, OB, row_b(k, i), ko)],
-            ]
-            for q in range(3):
-                r = g[3 * t + q]
-                r["nseg"] = 4
-                for s, (am, ax, bm, brow, nk) in enumerate(segs[q]):
-                    r["amap"][s] = am
-                    r["arow"][s] = ax * v2
-                    r["bmap"][s] = bm
-                    r["brow"][s] = brow
-                    r["nkb"][s] = nk
-                r["out"] = (3 * t + q) * v3
+        # per orientation: four (A map, A triple index, B map, B row, K blocks) segments
+        segs = [
+            [(VT, i, T2P, row_b(k, j), kv), (VN, j, T2P, row_b(k, i), kv),
+             (TM, i, OB, row_b(j, k), ko), (TMT, j, OB, row_b(i, k), ko)],
+            [(VT, i, T2P, row_b(j, k), kv), (VN, k, T2P, row_b(j, i), kv),
+             (TM, i, OB, row_b(k, j), ko), (TMT, k, OB, row_b(i, j), ko)],
+            [(VN, k, T2P, row_b(i, j), kv), (VT, j, T2P, row_b(i, k), kv),
+             (TMT, k, OB, row_b(j, i), ko), (TM, j, OB, row_b(k, i), ko)],
+        ]
+        t = np.arange(nt)
+        for q in range(3):
+            r = g[q::3]
+            r["nseg"] = 4
+            for s, (am, ax, bm, brow, nk) in enumerate(segs[q]):
+                r["amap"][:, s] = am
+                r["arow"][:, s] = ax * v2
+                r["bmap"][:, s] = bm
+                r["brow"][:, s] = brow
+                r["nkb"][:, s] = nk
+            r["out"] = (3 * (t % self.batch) + q) * v3
         return g
 
     def energy(self):
@@ -117,17 +122,18 @@ class TriplesTC:
         fov = H.F[o, v].contiguous()
         fov_ptr = fov.data_ptr() if bool(fov.abs().max() > 0) else None
         eoovv = H.ERI[o, o, v, v]
+        # every batch's group records, uploaded once; a batch's partials start at P[0]
+        gall = torch.from_numpy(self.groups(trips).view(np.uint8)).to(dev)
+        gsz = GROUP_DTYPE.itemsize
         for b0 in range(0, len(trips), nb):
             chunk = trips[b0:b0 + nb]
-            gt = torch.from_numpy(self.groups(chunk).view(np.uint8)).to(dev)
             _lib.call("pcg_tc_grouped_gemm", 4, a_ptr, a_rows, a_ld, 2, b_ptr, b_rows, b_ld,
-                      gt.data_ptr(), 3 * len(chunk), nv * nv, nv, P.data_ptr(), nv,
-                      self.status.data_ptr(), st)
+                      gall.data_ptr() + 3 * b0 * gsz, 3 * len(chunk), nv * nv, nv,
+                      P.data_ptr(), 1, nv * nv, self.status.data_ptr(), st)
             _lib.call("pcg_triples_energy", 1, P.data_ptr(), P[:, 1].data_ptr(),
                       P[:, 2].data_ptr(), 3 * nv ** 3, ijk_all[b0:].data_ptr(), len(chunk),
                       H.eps.data_ptr(), eoovv.data_ptr(), self.t1.data_ptr(), self.t2.data_ptr(),
                       fov_ptr, no, nv, part[b0:].data_ptr(), st)
-            del gt
         out = torch.zeros((), dtype=torch.float64, device=dev)
         _lib.call("pcg_reduce_sum_f64", part.data_ptr(), part.numel(), out.data_ptr(), st)
         s = self.status.cpu()

@@ -10,21 +10,22 @@ import pytest
 import torch
 
 import pycc_gb300 as pg
-from pycc_gb300.tc import FMT_BF16, FMT_BF16X3, FMT_FP8, Operand, TCEngine
+from pycc_gb300.tc import FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_FP8, Operand, TCEngine
 from oracle import ccsd as oc
 
 pytestmark = pytest.mark.gpu
-TOL = {FMT_BF16: 2e-2, FMT_BF16X3: 5e-5, FMT_FP8: 8e-2}
+TOL = {FMT_BF16: 2e-2, FMT_BF16X3: 5e-5, FMT_BF16X3F: 5e-5, FMT_FP8: 8e-2}
 
 
 def frob(a, b):
     return (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
 
 
-@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_FP8])
+@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_FP8])
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (200, 70, 100), (37, 300, 513), (64, 180, 96),
                                    (100, 210, 64), (150, 150, 64), (300, 820, 200)])
 def test_gemm_exact_integers(cuda, fmt, M, N, K):
+    """N = 70, 150, 180, 210, 820 select the 96-, 160-, 192- and 224-column tiles."""
     g = torch.Generator(device=cuda).manual_seed(M + N + K)
     A = torch.randint(-3, 4, (M, K), generator=g, device=cuda).double()
     B = torch.randint(-3, 4, (N, K), generator=g, device=cuda).double()
@@ -40,7 +41,7 @@ def test_gemm_exact_integers(cuda, fmt, M, N, K):
     assert torch.equal(out, ref)
 
 
-@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_FP8])
+@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_FP8])
 def test_gemm_random_error(cuda, fmt):
     g = torch.Generator(device=cuda).manual_seed(5)
     A = torch.randn(333, 1000, generator=g, device=cuda, dtype=torch.float64)

@@ -64,8 +64,11 @@ def test_ccsd_t_model(cuda, cfg1_ham, cfg1):
     assert abs(e - (float(cfg1["ecc"]) + float(cfg1["et_tjl"]))) < 1e-10
 
 
-def test_grouped_gemm_exact(cuda):
-    """Two groups with two K segments each, integer data: exact against torch."""
+@pytest.mark.parametrize("layout", ["row", "col"])
+def test_grouped_gemm_exact(cuda, layout):
+    """Two groups with two K segments each, integer data: exact against torch, with the
+    output row-major (ldm=N, ldn=1) or column-major (ldm=1, ldn=M, the (T) layout).  N=150
+    takes the 160-wide tile (a 16-column remainder per epilogue warp)."""
     g = torch.Generator(device=cuda).manual_seed(3)
     M, N = 300, 150
     A0 = torch.randint(-3, 4, (2 * M, 64), generator=g, device=cuda).double()
@@ -85,15 +88,19 @@ def test_grouped_gemm_exact(cuda):
     gd[1]["nkb"][0] = 1
     gd[1]["out"] = M * N
     gt = torch.from_numpy(gd.view(np.uint8)).to(cuda)
-    out = torch.full((2, M, N), float("nan"), dtype=torch.float32, device=cuda)
+    shape = (2, M, N) if layout == "row" else (2, N, M)
+    ldm, ldn = (N, 1) if layout == "row" else (1, M)
+    out = torch.full(shape, float("nan"), dtype=torch.float32, device=cuda)
     st = torch.zeros(4, dtype=torch.int32, device=cuda)
     a_ptr = (C.c_void_p * 2)(*[x.hi.data_ptr() for x in pa])
     b_ptr = (C.c_void_p * 2)(*[x.hi.data_ptr() for x in pb])
     _lib.call("pcg_tc_grouped_gemm", 2, a_ptr, _lib.i64s([x.rows for x in pa]),
               _lib.i64s([x.Kp for x in pa]), 2, b_ptr, _lib.i64s([x.rows for x in pb]),
-              _lib.i64s([x.Kp for x in pb]), gt.data_ptr(), 2, M, N, out.data_ptr(), N,
+              _lib.i64s([x.Kp for x in pb]), gt.data_ptr(), 2, M, N, out.data_ptr(), ldm, ldn,
               st.data_ptr(), _lib.stream_handle())
     torch.cuda.synchronize()
+    if layout == "col":
+        out = out.transpose(1, 2)
     ref0 = A0[:M] @ B0[:N].T + A1 @ B1[N:].T
     ref1 = A0[M:] @ B0[20:20 + N].T
     assert torch.equal(out[0].double(), ref0)
