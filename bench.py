@@ -170,7 +170,7 @@ def triples_mode(args, dev):
     import torch
     import pycc_gb300 as pg
     from pycc_gb300.triples_tc import t_energy_tc
-    no, nv, seed = 30, 240, 4
+    no, nv, seed = (30, 240, 4) if args.triples_size is None else tuple(args.triples_size)
     fac = pg.SyntheticFactors(no, nv, seed, coupling="matched")
     H = pg.Hamiltonian.from_factors(fac, device=dev)
     w = pg.CCwfn(H, precision="MIXED")
@@ -324,6 +324,8 @@ def main():
                     help="ccsd: the benchmark line; triples / adjoint: the (T) and adjoint "
                          "measurements at no=30,nv=240 and no=20,nv=180; term: one residual "
                          "contraction (--term) alone at --no/--nv")
+    ap.add_argument("--triples-size", type=int, nargs=3, default=None, metavar=("NO", "NV", "SEED"),
+                    help="(T) mode at another size (profiling; the measurement is no=30,nv=240)")
     ap.add_argument("--term", default="nb,mnej->mbej")
     ap.add_argument("--term-fmt", default="bf16x3f", choices=["bf16", "bf16x3", "bf16x3f"])
     args = ap.parse_args()

@@ -130,16 +130,23 @@ int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n
 /* ---- (T) ---------------------------------------------------------------------------
  * Lee-Rendell E(T) of the reference's t_tjl (pycc/cctriples.py:177-240) for ntrip triples
  * ijk[t] = (i, j, k), i >= j >= k.  The connected triples of triple t are given as three
- * partial tensors (v^3 each, pstride elements apart between triples):
- *   W[a,b,c] = P1[a][b][c] + P2[a][c][b] + P3[b][c][a]
+ * partial tensors (v^3 each, pstride elements apart between triples), column-major GEMM
+ * outputs of the three term orientations:
+ *   W[a,b,c] = P1[c][a][b] + P2[b][a][c] + P3[a][b][c]
  * the disconnected triples (t3d_ijk, :108-147) are formed from eoovv = <ij|ab>, t1 and, if
- * fov is not NULL, t2 and f_ov.  fp32 != 0: FP32 partials and element arithmetic, else
- * FP64.  Writes part[t*nv + a] (FP64, weight (2 - d_ij - d_ik - d_jk) applied). */
+ * fov is not NULL, t2 and f_ov.  fp32 != 0: FP32 partials, eoovv and t2 (16-byte aligned)
+ * and FP32 element arithmetic (tiles of the (a, b, c) cube); else all FP64.  eps, t1 and
+ * fov are FP64 in both.  Writes pcg_triples_part_len(fp32, nv) FP64 partials per
+ * triple at part[t * len ...] (weight (2 - d_ij - d_ik - d_jk) applied); E(T) is their sum. */
 int pcg_triples_energy(int fp32, const void* P1, const void* P2, const void* P3,
                        long long pstride, const int* ijk, int ntrip, const double* eps,
-                       const double* eoovv, const double* t1, const double* t2,
+                       const void* eoovv, const double* t1, const void* t2,
                        const double* fov, long long no, long long nv, double* part,
                        void* stream);
+/* FP64 partials per triple written by pcg_triples_energy: nv (FP64), or the number of
+ * 8^3 tile triples A >= B >= C of the virtual range (FP32).  (Sizing helper, no reference
+ * counterpart.) */
+long long pcg_triples_part_len(int fp32, long long nv);
 /* *out += sum(x[0:n]) in FP64 (one block, deterministic). */
 int pcg_reduce_sum_f64(const double* x, long long n, double* out, void* stream);
 

@@ -44,6 +44,7 @@ SIGNATURES = {
                                          _p]),
     "pcg_triples_energy": (C.c_int, [C.c_int, _p, _p, _p, _i64, _p, C.c_int, _p, _p, _p, _p, _p,
                                      _i64, _i64, _p, _p]),
+    "pcg_triples_part_len": (C.c_longlong, [C.c_int, _i64]),
     "pcg_reduce_sum_f64": (C.c_int, [_p, _i64, _p, _p]),
     "pcg_tc_grouped_gemm": (C.c_int, [C.c_int, C.POINTER(_p), _pi64, _pi64, C.c_int, C.POINTER(_p),
                                       _pi64, _pi64, _p, C.c_int, _i64, _i64, _p, _i64, _i64, _p,

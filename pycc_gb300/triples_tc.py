@@ -107,7 +107,9 @@ class TriplesTC:
         trips = triples_list(no)
         nb = self.batch
         P = torch.empty((nb, 3, nv, nv, nv), dtype=torch.float32, device=dev)
-        part = torch.empty((len(trips), nv), dtype=torch.float64, device=dev)
+        plen = int(_lib.load().pcg_triples_part_len(1, nv))
+        part = torch.empty((nb, plen), dtype=torch.float64, device=dev)   # one batch
+        out = torch.zeros((), dtype=torch.float64, device=dev)
         ijk_all = torch.tensor(trips, dtype=torch.int32, device=dev)
         st = _lib.stream_handle(w.stream)
         A, B = self.A, self.B
@@ -121,7 +123,8 @@ class TriplesTC:
         o, v = w.o, w.v
         fov = H.F[o, v].contiguous()
         fov_ptr = fov.data_ptr() if bool(fov.abs().max() > 0) else None
-        eoovv = H.ERI[o, o, v, v]
+        eoovv = H.ERI[o, o, v, v].float()          # the FP32 energy kernel's copies
+        t2f = self.t2.float()
         # every batch's group records, uploaded once; a batch's partials start at P[0]
         gall = torch.from_numpy(self.groups(trips).view(np.uint8)).to(dev)
         gsz = GROUP_DTYPE.itemsize
@@ -132,10 +135,10 @@ class TriplesTC:
                       P.data_ptr(), 1, nv * nv, self.status.data_ptr(), st)
             _lib.call("pcg_triples_energy", 1, P.data_ptr(), P[:, 1].data_ptr(),
                       P[:, 2].data_ptr(), 3 * nv ** 3, ijk_all[b0:].data_ptr(), len(chunk),
-                      H.eps.data_ptr(), eoovv.data_ptr(), self.t1.data_ptr(), self.t2.data_ptr(),
-                      fov_ptr, no, nv, part[b0:].data_ptr(), st)
-        out = torch.zeros((), dtype=torch.float64, device=dev)
-        _lib.call("pcg_reduce_sum_f64", part.data_ptr(), part.numel(), out.data_ptr(), st)
+                      H.eps.data_ptr(), eoovv.data_ptr(), self.t1.data_ptr(), t2f.data_ptr(),
+                      fov_ptr, no, nv, part.data_ptr(), st)
+            _lib.call("pcg_reduce_sum_f64", part.data_ptr(), len(chunk) * plen, out.data_ptr(),
+                      st)
         s = self.status.cpu()
         if int(s.abs().sum()):
             raise _lib.EngineError("grouped GEMM reported a wait timeout (status %s)" % s.tolist())
