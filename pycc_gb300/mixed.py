@@ -23,7 +23,7 @@ import torch
 from . import _lib
 from .contract import contract_f64
 from .tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X6, FMT_FP8, Operand, TCEngine, pack,
-                 pack_format)
+                 static_pack_format)
 
 
 class MixedResidual:
@@ -90,7 +90,7 @@ class MixedResidual:
         """Free the packed integrals of formats no remaining stage reads."""
         used = set()
         for name in self.stages[self.stage:]:
-            used.add(pack_format(self.FMTS[name]))
+            used.add(static_pack_format(self.FMTS[name]))
             if name == "fp8":
                 used.add(FMT_FP8)
         for key in [k for k in self.tc.cache if k[-1] not in used]:

@@ -26,6 +26,15 @@ FMT_BF16, FMT_BF16X3, FMT_FP8, FMT_BF16X6, FMT_BF16X3F = 0, 1, 2, 3, 4
 def pack_format(fmt):
     """The operand pieces a GEMM format reads (fused and by-pass split-BF16x3 share them)."""
     return FMT_BF16X3 if fmt == FMT_BF16X3F else fmt
+
+
+def static_pack_format(fmt):
+    """The pieces cached for a static operand (an integral block).  A BF16 GEMM keeps the
+    split-BF16x3 pair: its hi piece is the BF16 operand bit for bit (the same rounding of
+    the same FP32 value), and the split-BF16x3 stages then reuse the cached pack instead of
+    packing every integral block again."""
+    f = pack_format(fmt)
+    return FMT_BF16X3 if f == FMT_BF16 else f
 MAX_SUB = 4
 
 
@@ -259,10 +268,11 @@ class TCEngine:
                 self.dyn_cache[dkey] = p
             return p
         # the operand's own label string fixes which tensor axis each label names
-        key = (op.key, op.labels, tuple(rows), tuple(ks), pack_format(fmt))
+        sf = static_pack_format(fmt)
+        key = (op.key, op.labels, tuple(rows), tuple(ks), sf)
         p = self.cache.get(key)
         if p is None:
-            p = pack(op, rows, ks, fmt, self.stream)
+            p = pack(op, rows, ks, sf, self.stream)
             self.cache[key] = p
         return p
 
