@@ -35,6 +35,11 @@ METRIC = "CCSD s/iter & TFLOP/s (no=40,nv=300): mixed vs FP64 on GB300 at 1e-6 E
 FP64_REF = os.path.join(ROOT, "tests", "golden", "fp64_reference.json")
 
 
+# (no, nv, GEMM format) -> DRAM bytes of one ladder launch, from a one-pass ncu capture
+# (81.02 GB read + 12.80 GB written at no=40, nv=300, fused split-BF16x3)
+LADDER_DRAM_BYTES = {(40, 300, 4): 93.82e9}
+
+
 def f_iter(o, v):
     return 2 * o**2 * v**4 + 18 * o**3 * v**3 + 10 * o**2 * v**3 + 4 * o**4 * v**2
 
@@ -435,8 +440,12 @@ def main():
         work = npass * 2.0 * pairs * v_n**4
         achieved = work / (lr["ms"] * 1e-3) / 1e12
         padded = npass * 2.0 * lr["M"] * lr["N"] * lr["Kp"] / (lr["ms"] * 1e-3) / 1e12
+        # DRAM bytes of this launch (dram__bytes_read.sum + dram__bytes_write.sum) from a
+        # one-pass ncu capture of the fused-stage ladder at this size, 128 x 224 tiles
+        traffic = LADDER_DRAM_BYTES.get((o_n, v_n, lr["fmt"]))
         roofline = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16"],
-                    "unit": "TFLOP/s", "frac": achieved / pk["bf16"], "traffic": None,
+                    "unit": "TFLOP/s", "frac": achieved / pk["bf16"], "traffic": traffic,
+                    "traffic_unit": "bytes per launch (ncu capture)" if traffic else None,
                     "kernel": "tc_gemm_kernel ladder ijef,abef->ijab (i<=j pairs)",
                     "mode": {0: "bf16", 1: "bf16x3", 2: "fp8", 3: "bf16x6", 4: "bf16x3f"}[lr["fmt"]],
                     "work_per_launch_flop": work, "passes": npass,
