@@ -109,6 +109,23 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_time(ms, world, device):
+    """The per-step time of the job: the slowest of the ``world`` replicas (each rank runs
+    the whole iteration on its own GPU; no data-path collective)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms
+
+
+def job_tflops(flop_per_step, ms, world):
+    """Whole-job rate: every replica does flop_per_step per step of ms milliseconds."""
+    return world * flop_per_step / (ms * 1e-3) / 1e12
+
+
 def dist_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -396,11 +413,7 @@ def main():
     torch.cuda.synchronize()
     launches = _lib.launch_count() - l0
     clocks = clk.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replica_time(ev0.elapsed_time(ev1) / args.steps, world, dev)
     modes = w.mixed_engine().history[-args.steps:]
     iter_ms = [round(x * 1e3, 2) for x in w.iter_times[-args.steps:]]
     timed_energy = w.energies[-1]
@@ -477,7 +490,7 @@ def main():
         e2e_step()
     e1.record()
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / max(args.e2e_steps, 1)
+    e2e_ms = replica_time(e0.elapsed_time(e1) / max(args.e2e_steps, 1), world, dev)
     nb = (t1h.numel() + t2h.numel()) * 8
 
     # ---- plain FP64 form at the same size --------------------------------------------------
@@ -516,7 +529,7 @@ def main():
                "sample": res["sample"]}
 
     line = {
-        "metric": METRIC, "value": F_it / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+        "metric": METRIC, "value": job_tflops(F_it, ms, world), "unit": "TFLOP/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16", "data": "synthetic",
@@ -528,8 +541,8 @@ def main():
         "s_per_iter": ms * 1e-3, "modes_timed": modes, "iter_wall_ms": iter_ms, "energy_timed_last": timed_energy,
         "energy_mixed": e_mixed, "energy_error_vs_fp64": err,
         "fp64": fp64, "roofline": roofline, "cpu_baseline": cpu,
-        "e2e": {"value": F_it / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
-                "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb,
+        "e2e": {"value": job_tflops(F_it, e2e_ms, world), "unit": "TFLOP/s",
+                "h2d_bytes_per_step": world * nb, "d2h_bytes_per_step": world * nb,
                 "what": "CCwfn.residuals with pinned-host t1/t2 in and r1/r2 out",
                 "ms_per_step": e2e_ms},
         "gpu_launches": launches, "clocks": clocks, "setup_s": setup_s,
