@@ -126,6 +126,13 @@ int pcg_diis_error_f32(const double* x, const double* old, float* e, const float
  * DIIS extrapolation, helper_diis.extrapolate (pycc/utils.py:351-355) */
 int pcg_lincomb_f64(const double* const* xs, const double* c, int k, long long n, double* out,
                     void* stream);
+/* pcg_lincomb_f64 in double-float arithmetic, for the mixed-precision solver: every FP64
+ * input split into FP32 hi + lo pieces in integer arithmetic, products with their FMA
+ * rounding errors, the sum carried as an FP32 pair; about 48 significant bits, one FP64
+ * instruction per element instead of k.  Inputs and output 16-byte aligned.  The same DIIS
+ * extrapolation (pycc/utils.py:351-355). */
+int pcg_lincomb_f64_df(const double* const* xs, const double* c, int k, long long n,
+                       double* out, void* stream);
 
 /* ---- (T) ---------------------------------------------------------------------------
  * Lee-Rendell E(T) of the reference's t_tjl (pycc/cctriples.py:177-240) for ntrip triples

@@ -36,6 +36,7 @@ SIGNATURES = {
     "pcg_dots_f64": (C.c_int, [_p, C.POINTER(_p), C.c_int, _i64, _p, _i64, _p, _p]),
     "pcg_dots_f64_noalloc": (C.c_int, [_p, C.POINTER(_p), C.c_int, _i64, _p, _p]),
     "pcg_lincomb_f64": (C.c_int, [C.POINTER(_p), C.POINTER(_d), C.c_int, _i64, _p, _p]),
+    "pcg_lincomb_f64_df": (C.c_int, [C.POINTER(_p), C.POINTER(_d), C.c_int, _i64, _p, _p]),
     "pcg_diis_error_f64": (C.c_int, [_p, _p, _p, C.POINTER(_p), C.c_int, _i64, _p, _i64, _p, _p]),
     "pcg_diis_error_f32": (C.c_int, [_p, _p, _p, C.POINTER(_p), C.c_int, _i64, _p, _i64, _p, _p]),
     "pcg_contract_multi_f64": (C.c_int, [C.c_int, C.c_int, _pi64, _pi64, _pi64, C.c_int, _pi64,

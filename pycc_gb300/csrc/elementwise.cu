@@ -47,10 +47,12 @@ __global__ void tau_kernel(const double* __restrict__ t1, const double* __restri
   long long total = no * no * nv * nv;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
-    long long b = idx % nv, r = idx / nv;
-    long long a = r % nv;
-    r /= nv;
-    long long j = r % no, i = r / no;
+    unsigned r = (unsigned)idx;  // o^2 v^2 < 2^31 (host check)
+    const long long b = r % (unsigned)nv;
+    r /= (unsigned)nv;
+    const long long a = r % (unsigned)nv;
+    r /= (unsigned)nv;
+    const long long j = r % (unsigned)no, i = r / (unsigned)no;
     double x = f1 * t2[idx];
     if (f2 != 0.0) x += f2 * t1[i * nv + a] * t1[j * nv + b];
     out[idx] = x;
@@ -61,16 +63,20 @@ struct Strides4 {
   long long e[4], x[4], y[4], o[4];
 };
 
+// I: the index type of the decomposition (unsigned when the tensor has < 2^31 elements;
+// 64-bit division is several times longer)
+template <typename I>
 __global__ void combine4_kernel(Strides4 s, double a, const double* __restrict__ X, double b,
                                 const double* __restrict__ Y, double* __restrict__ out) {
   long long total = s.e[0] * s.e[1] * s.e[2] * s.e[3];
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
-    long long r = idx, ox = 0, oy = 0, oo = 0;
+    I r = (I)idx;
+    long long ox = 0, oy = 0, oo = 0;
 #pragma unroll
     for (int q = 3; q >= 0; --q) {
-      long long c = r % s.e[q];
-      r /= s.e[q];
+      const long long c = r % (I)s.e[q];
+      r /= (I)s.e[q];
       ox += c * s.x[q];
       oy += c * s.y[q];
       oo += c * s.o[q];
@@ -86,10 +92,12 @@ __global__ void symmetrize_kernel(const double* __restrict__ h, long long no, lo
   long long total = no * no * nv * nv;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
-    long long b = idx % nv, r = idx / nv;
-    long long a = r % nv;
-    r /= nv;
-    long long j = r % no, i = r / no;
+    unsigned r = (unsigned)idx;  // o^2 v^2 < 2^31 (host check)
+    const long long b = r % (unsigned)nv;
+    r /= (unsigned)nv;
+    const long long a = r % (unsigned)nv;
+    r /= (unsigned)nv;
+    const long long j = r % (unsigned)no, i = r / (unsigned)no;
     out[idx] = h[idx] + h[((j * no + i) * nv + b) * nv + a];
   }
 }
@@ -103,16 +111,19 @@ __global__ void update_kernel(double* __restrict__ t1, double* __restrict__ t2,
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
     if (idx < n1) {
-      long long a = idx % nv, i = idx / nv;
+      const unsigned x = (unsigned)idx;  // o^2 v^2 < 2^31 (host check)
+      const long long a = x % (unsigned)nv, i = x / (unsigned)nv;
       double u = r1[idx] / (eps[i] - eps[no + a]);
       t1[idx] += u;
       acc += u * u;
     } else {
-      long long q = idx - n1;
-      long long b = q % nv, r = q / nv;
-      long long a = r % nv;
-      r /= nv;
-      long long j = r % no, i = r / no;
+      const long long q = idx - n1;
+      unsigned r = (unsigned)q;
+      const long long b = r % (unsigned)nv;
+      r /= (unsigned)nv;
+      const long long a = r % (unsigned)nv;
+      r /= (unsigned)nv;
+      const long long j = r % (unsigned)no, i = r / (unsigned)no;
       double u = r2[q] / (eps[i] + eps[j] - eps[no + a] - eps[no + b]);
       t2[q] += u;
       acc += u * u;
@@ -165,15 +176,20 @@ __global__ void energy_kernel(const double* __restrict__ fov, long long fs0, lon
   double acc = 0.0;
   for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (long long)gridDim.x * blockDim.x) {
+    // index decomposition in 32-bit arithmetic (o^2 v^2 < 2^31, checked by the host)
+    const unsigned v32 = (unsigned)nv, o32 = (unsigned)no;
     if (idx < n1) {
-      long long a = idx % nv, i = idx / nv;
+      const unsigned x = (unsigned)idx;
+      const long long a = x % v32, i = x / v32;
       acc += 2.0 * fov[i * fs0 + a * fs1] * t1[idx];
     } else {
-      long long q = idx - n1;
-      long long b = q % nv, r = q / nv;
-      long long a = r % nv;
-      r /= nv;
-      long long j = r % no, i = r / no;
+      const long long q = idx - n1;
+      unsigned r = (unsigned)q;
+      const long long b = r % v32;
+      r /= v32;
+      const long long a = r % v32;
+      r /= v32;
+      const long long j = r % o32, i = r / o32;
       double tau = t2[q] + t1[i * nv + a] * t1[j * nv + b];
       acc += tau * L[i * ls.o[0] + j * ls.o[1] + a * ls.o[2] + b * ls.o[3]];
     }
@@ -298,6 +314,74 @@ __global__ void lincomb_kernel(VecList xs, int k, long long n, double* __restric
   }
 }
 
+// x = hi + lo with hi the FP32 rounding of x and lo the FP32 rounding of the remainder
+// x - hi, both in integer arithmetic: hi keeps the top 24 of the 53 significand bits, lo the
+// next 24 (remainders of FP64 values below 2^-74 in magnitude flush to zero).
+__device__ __forceinline__ void split_f64(double x, float& hi, float& lo) {
+  hi = f64_to_f32(x);
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned uh = (unsigned)(u >> 32), ul = (unsigned)u;
+  const int ex = (int)((uh >> 20) & 0x7ffu);
+  const unsigned m = ((uh & 0xfffffu) << 3) | (ul >> 29);
+  const int rest = (int)(ul & 0x1fffffffu);  // the 29 bits hi dropped
+  const bool up = rest > 0x10000000 || (rest == 0x10000000 && (m & 1u));
+  const int r = up ? rest - 0x20000000 : rest;  // x - hi in units of 2^(e - 52)
+  const int e2 = ex - 1023 - 52 + 127;          // FP32 exponent field of 2^(e - 52)
+  float lo_ = 0.f;
+  if (ex != 0 && ex != 0x7ff && e2 > 0 && e2 < 255)
+    lo_ = __int2float_rn(r) * __uint_as_float((unsigned)e2 << 23);
+  lo = (uh & 0x80000000u) ? -lo_ : lo_;
+}
+
+// out = sum_j c_j x_j in double-float arithmetic: each term's FP32 pieces and the
+// coefficient's (c_hi, c_lo) give the product with its exact rounding error (FMA), the
+// running sum is kept as an unevaluated FP32 pair (TwoSum), about 48 significant bits; one
+// FP64 addition per element assembles the result.
+__device__ __forceinline__ void df_term(double x, float ch, float cl, float& S, float& E) {
+  float h, l;
+  split_f64(x, h, l);
+  const float p = ch * h;
+  float e = fmaf(ch, h, -p);
+  e = fmaf(ch, l, e);
+  e = fmaf(cl, h, e);
+  const float t = S + p;
+  const float bp = t - S;
+  E += ((S - (t - bp)) + (p - bp)) + e;
+  S = t;
+}
+
+// Two elements per step through 16-byte loads (the inputs and the output are 16-byte
+// aligned, checked by the host); the last element of an odd n is done by one thread.
+__global__ void lincomb_df_kernel(VecList xs, int k, long long n, double* __restrict__ out) {
+  float ch[kMaxVec], cl[kMaxVec];
+#pragma unroll
+  for (int j = 0; j < kMaxVec; ++j) {
+    ch[j] = (float)xs.c[j];
+    cl[j] = (float)(xs.c[j] - (double)ch[j]);
+  }
+  const long long n2 = n >> 1;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n2;
+       q += (long long)gridDim.x * blockDim.x) {
+    float S0 = 0.f, E0 = 0.f, S1 = 0.f, E1 = 0.f;
+#pragma unroll
+    for (int j = 0; j < kMaxVec; ++j)
+      if (j < k) {
+        const double2 x = reinterpret_cast<const double2*>(xs.p[j])[q];
+        df_term(x.x, ch[j], cl[j], S0, E0);
+        df_term(x.y, ch[j], cl[j], S1, E1);
+      }
+    reinterpret_cast<double2*>(out)[q] =
+        make_double2(f32_to_f64(S0) + f32_to_f64(E0), f32_to_f64(S1) + f32_to_f64(E1));
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    float S = 0.f, E = 0.f;
+#pragma unroll
+    for (int j = 0; j < kMaxVec; ++j)
+      if (j < k) df_term(xs.p[j][n - 1], ch[j], cl[j], S, E);
+    out[n - 1] = f32_to_f64(S) + f32_to_f64(E);
+  }
+}
+
 bool check_work(long long work_len, long long need, const char* who) {
   if (work_len < need) {
     set_error("%s: work buffer holds %lld doubles, needs %lld", who, work_len, need);
@@ -313,8 +397,8 @@ using namespace pcg;
 
 extern "C" int pcg_tau_f64(const double* t1, const double* t2, long long no, long long nv,
                            double f1, double f2, double* out, void* stream) {
-  if (!t1 || !t2 || !out || no <= 0 || nv <= 0) {
-    set_error("pcg_tau_f64: bad arguments");
+  if (!t1 || !t2 || !out || no <= 0 || nv <= 0 || no * no * nv * nv > 0x7fffffffLL) {
+    set_error("pcg_tau_f64: bad arguments (o^2 v^2 must be below 2^31)");
     return -1;
   }
   long long n = no * no * nv * nv;
@@ -344,7 +428,12 @@ extern "C" int pcg_combine4_f64(const long long* ext, double a, const double* X,
     }
     n *= ext[q];
   }
-  combine4_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(s, a, X, b, Y, out);
+  if (n <= 0x7fffffffLL)
+    combine4_kernel<unsigned><<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(s, a, X, b,
+                                                                                    Y, out);
+  else
+    combine4_kernel<unsigned long long>
+        <<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(s, a, X, b, Y, out);
   PCG_CHECK_LAUNCH("pcg_combine4_f64");
   return 0;
 }
@@ -353,6 +442,10 @@ extern "C" int pcg_symmetrize_f64(const double* h, long long no, long long nv, d
                                   void* stream) {
   if (!h || !out || h == out) {
     set_error("pcg_symmetrize_f64: bad pointers (input and output must differ)");
+    return -1;
+  }
+  if (no <= 0 || nv <= 0 || no * no * nv * nv > 0x7fffffffLL) {
+    set_error("pcg_symmetrize_f64: o^2 v^2 must be in [1, 2^31)");
     return -1;
   }
   long long n = no * no * nv * nv;
@@ -365,6 +458,10 @@ extern "C" int pcg_update_amps_f64(double* t1, double* t2, const double* r1, con
                                    const double* eps, long long no, long long nv, double* work,
                                    long long work_len, double* rms2, void* stream) {
   if (!check_work(work_len, RED_BLOCKS, "pcg_update_amps_f64")) return -1;
+  if (no <= 0 || nv <= 0 || no * no * nv * nv > 0x7fffffffLL) {
+    set_error("pcg_update_amps_f64: o^2 v^2 must be in [1, 2^31)");
+    return -1;
+  }
   cudaStream_t st = (cudaStream_t)stream;
   long long n = no * nv + no * no * nv * nv;
   int nb = std::min(ew_blocks(n), RED_BLOCKS);
@@ -383,6 +480,10 @@ extern "C" int pcg_energy_f64(const double* fov, const long long* fs, const doub
   cudaStream_t st = (cudaStream_t)stream;
   Strides4 s{};
   for (int q = 0; q < 4; ++q) s.o[q] = ls[q];
+  if (no < 1 || nv < 1 || no * no * nv * nv > 0x7fffffffLL) {
+    set_error("pcg_energy_f64: o^2 v^2 must be in [1, 2^31)");
+    return -1;
+  }
   long long n = no * nv + no * no * nv * nv;
   int nb = std::min(ew_blocks(n), RED_BLOCKS);
   energy_kernel<<<nb, EW_THREADS, 0, st>>>(fov, fs[0], fs[1], L, s, t1, t2, no, nv, work);
@@ -427,6 +528,35 @@ extern "C" int pcg_lincomb_f64(const double* const* xs, const double* c, int k, 
   }
   lincomb_kernel<<<ew_blocks(n), EW_THREADS, 0, (cudaStream_t)stream>>>(v, k, n, out);
   PCG_CHECK_LAUNCH("pcg_lincomb_f64");
+  return 0;
+}
+
+// pcg_lincomb_f64 in double-float arithmetic (see lincomb_df_kernel), for the
+// mixed-precision solver: one FP64 instruction per element instead of k.
+extern "C" int pcg_lincomb_f64_df(const double* const* xs, const double* c, int k, long long n,
+                                  double* out, void* stream) {
+  if (k < 1 || k > kMaxVec || !xs || !c || !out || n < 0) {
+    set_error("pcg_lincomb_f64_df: bad arguments (k=%d)", k);
+    return -1;
+  }
+  VecList v{};
+  bool aligned = ((uintptr_t)out & 15u) == 0;
+  for (int j = 0; j < k; ++j) {
+    if (!xs[j] || xs[j] == out) {
+      set_error("pcg_lincomb_f64_df: input %d is null or aliases the output", j);
+      return -1;
+    }
+    aligned = aligned && ((uintptr_t)xs[j] & 15u) == 0;
+    v.p[j] = xs[j];
+    v.c[j] = c[j];
+  }
+  if (!aligned) {
+    set_error("pcg_lincomb_f64_df: vectors must be 16-byte aligned");
+    return -1;
+  }
+  lincomb_df_kernel<<<ew_blocks(std::max(n / 2, 1LL)), EW_THREADS, 0, (cudaStream_t)stream>>>(
+      v, k, n, out);
+  PCG_CHECK_LAUNCH("pcg_lincomb_f64_df");
   return 0;
 }
 

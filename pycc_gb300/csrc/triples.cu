@@ -329,9 +329,11 @@ __global__ void __launch_bounds__(TE2_THREADS) triples_energy_tiled_kernel(
     const float D = eo - s.ev[la] - s.ev[lb] - s.ev[lc];
     acc += S / D;
   }
-  double dsum = (double)acc;
-  for (int sh = 16; sh > 0; sh >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, sh);
-  if ((tid & 31) == 0) s.red[tid >> 5] = dsum;
+  // warp sums as an FP32 tree (a few combinations per thread), the block's eight warp
+  // sums in FP64
+  float wsum = acc;
+  for (int sh = 16; sh > 0; sh >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, sh);
+  if ((tid & 31) == 0) s.red[tid >> 5] = f32_to_f64(wsum);
   __syncthreads();
   if (tid < 32) {
     double r = (tid < TE2_THREADS / 32) ? s.red[tid] : 0.0;

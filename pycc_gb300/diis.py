@@ -9,7 +9,8 @@ scaled by its largest |B| entry (``utils.py:341``) and solved in FP64; the new a
 
 With ``error_dtype=torch.float32`` (the mixed-precision solver) the error vectors are kept
 in FP32: each is the FP64 difference rounded once, and the overlaps come from FP32 products
-accumulated in FP64.  The amplitudes and their extrapolation stay FP64.
+accumulated in FP64.  The amplitudes stay FP64, and their extrapolation runs in
+double-float arithmetic (about 48 bits, one FP64 instruction per element).
 """
 from __future__ import annotations
 
@@ -76,7 +77,7 @@ class DIIS:
         c = np.linalg.solve(Bb, rhs)
         ptrs = (C.c_void_p * k)(*[x.data_ptr() for x in self.vals[1:]])
         coef = (C.c_double * k)(*[float(x) for x in c[:k]])
-        _lib.call("pcg_lincomb_f64", ptrs, coef, k, amps.numel(), amps.data_ptr(),
-                  _lib.stream_handle(self.stream))
+        fn = "pcg_lincomb_f64" if self.error_dtype == torch.float64 else "pcg_lincomb_f64_df"
+        _lib.call(fn, ptrs, coef, k, amps.numel(), amps.data_ptr(), _lib.stream_handle(self.stream))
         self.old = amps.clone()
         return amps

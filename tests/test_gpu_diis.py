@@ -99,3 +99,26 @@ def test_diis_fp32_errors_extrapolation(cuda):
     b = _run_gpu(t1s, t2s, cuda, torch.float32)
     for u, v in zip(a, b):
         assert np.abs(u - v).max() < 1e-4 * np.abs(u).max()
+
+
+@pytest.mark.parametrize("k,n", [(1, 1000), (3, 4099), (8, 1 << 20)])
+def test_lincomb_double_float(cuda, k, n):
+    """sum_j c_j x_j in double-float arithmetic against the FP64 sum: within 1e-13 of
+    sum_j |c_j x_j|, over magnitudes from 1e-12 to 1e6, signed zeros and DIIS-like
+    coefficients of both signs."""
+    g = torch.Generator(device=cuda).manual_seed(k * 7 + n)
+    xs = []
+    for j in range(k):
+        x = torch.randn(n, generator=g, dtype=torch.float64, device=cuda)
+        x *= torch.exp2(torch.randint(-40, 20, (n,), generator=g, device=cuda).double())
+        x[:4] = torch.tensor([0.0, -0.0, 1.0, -3.0], dtype=torch.float64)
+        xs.append(x)
+    c = np.array([(-1.0) ** j * (1.5 + j) for j in range(k)]) / k
+    out = torch.empty(n, dtype=torch.float64, device=cuda)
+    ptrs = (C.c_void_p * k)(*[x.data_ptr() for x in xs])
+    coef = (C.c_double * k)(*[float(v) for v in c])
+    _lib.call("pcg_lincomb_f64_df", ptrs, coef, k, n, out.data_ptr(), None)
+    torch.cuda.synchronize()
+    ref = sum(float(c[j]) * xs[j] for j in range(k))
+    scale = sum(abs(float(c[j])) * xs[j].abs() for j in range(k))
+    assert torch.all((out - ref).abs() <= 1e-13 * scale)
