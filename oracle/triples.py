@@ -6,7 +6,7 @@ A numpy restatement of the reference's closed-shell (T) drivers (CrawfordGroup/p
 a >= b >= c (``t_tjl`` :177-240), with the per-element Python loops of the reference
 replaced by whole-array numpy expressions over (a, b, c).  ``t_vikings`` (:243-308) is the
 full-(i, j, k) formulation, used to cross-check.  Pinned against the reference's own
-energies in ``tests/golden/cfg1.npz``.
+energies in ``tests/golden/o5v19.npz``.
 """
 from __future__ import annotations
 

@@ -5,12 +5,12 @@ running on hand-written sm_103a CUDA kernels behind a C ABI (``include/pycc_gb30
 """
 from .exceptions import PyCCError, InvalidKeywordError, ConvergenceError, NumericalError
 from .hamiltonian import Hamiltonian, BlockTensor
-from .synth import SyntheticFactors, CONFIGS, synthetic_factors
+from .synth import SyntheticFactors, WORKLOADS, synthetic_factors
 from .ccwfn import CCwfn, ccwfn
 from .contract import ContractionBackend, contract_f64
 
 __all__ = [
-    "CCwfn", "ccwfn", "Hamiltonian", "BlockTensor", "SyntheticFactors", "CONFIGS",
+    "CCwfn", "ccwfn", "Hamiltonian", "BlockTensor", "SyntheticFactors", "WORKLOADS",
     "synthetic_factors", "ContractionBackend", "contract_f64", "PyCCError",
     "InvalidKeywordError", "ConvergenceError", "NumericalError",
 ]

@@ -34,13 +34,16 @@ from __future__ import annotations
 
 import numpy as np
 
-#: The five workloads of the RHF-CCSD engine: (no, nv, seed).
-CONFIGS = {
-    1: (5, 19, 0),
-    2: (20, 180, 1),
-    3: (40, 300, 2),
-    4: (20, 180, 3),
-    5: (30, 240, 4),
+#: The synthetic workloads of the RHF-CCSD engine, named by size: (no, nv, seed).
+#: o5v19 is small enough for the reference itself (the golden vectors); o20v180 is the
+#: largest the reference's host arrays hold; o40v300 is the CCSD benchmark; o20v180s3 the
+#: adjoint measurement; o30v240 the (T) measurement.
+WORKLOADS = {
+    "o5v19": (5, 19, 0),
+    "o20v180": (20, 180, 1),
+    "o40v300": (40, 300, 2),
+    "o20v180s3": (20, 180, 3),
+    "o30v240": (30, 240, 4),
 }
 
 
@@ -107,6 +110,6 @@ def matched_coupling(no: int, nv: int, naux: int) -> float:
     return float((_REF_STRENGTH * naux / float(no * no * nv * nv)) ** 0.25)
 
 
-def synthetic_factors(config: int, coupling=1.0) -> SyntheticFactors:
-    no, nv, seed = CONFIGS[config]
+def synthetic_factors(name: str, coupling=1.0) -> SyntheticFactors:
+    no, nv, seed = WORKLOADS[name]
     return SyntheticFactors(no, nv, seed, coupling=coupling)

@@ -23,12 +23,12 @@ def golden(name):
 
 
 @pytest.fixture(scope="session")
-def cfg1():
-    return golden("cfg1.npz")
+def golden_o5v19():
+    return golden("o5v19.npz")
 
 
 @pytest.fixture(scope="session")
-def cfg1_ham():
+def ham_o5v19():
     from pycc_gb300.synth import SyntheticFactors
     fac = SyntheticFactors(5, 19, 0)
     F, ERI, L = fac.hamiltonian()

@@ -12,7 +12,7 @@ Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
 
 Usage::
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--cfg2]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180]
 
 Config 2 (no=20, nv=180) needs ~30 GB of host RAM and several minutes.
 """
@@ -32,7 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
-from pycc_gb300.synth import SyntheticFactors, CONFIGS  # noqa: E402
+from pycc_gb300.synth import SyntheticFactors, WORKLOADS  # noqa: E402
 
 
 def import_reference():
@@ -114,8 +114,8 @@ def quiet(fn, *args, **kwargs):
         return fn(*args, **kwargs)
 
 
-def gen_cfg1(pycc):
-    no, nv, seed = CONFIGS[1]
+def gen_o5v19(pycc):
+    no, nv, seed = WORKLOADS["o5v19"]
     fac = SyntheticFactors(no, nv, seed)
     F, ERI, L = fac.hamiltonian()
     w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
@@ -173,21 +173,21 @@ def gen_cfg1(pycc):
     out["D"] = np.asarray(D)
     out["Gamma"] = np.asarray(G)
     out["E_from_densities"] = float(np.sum(D * F) + np.sum(G * ERI))
-    np.savez_compressed(os.path.join(HERE, "cfg1.npz"), **out)
-    print("cfg1: ecc = %.15f  (T) = %.15f / %.15f  pseudo = %.15f  E(D,G) = %.15f  niter = %d"
+    np.savez_compressed(os.path.join(HERE, "o5v19.npz"), **out)
+    print("golden_o5v19: ecc = %.15f  (T) = %.15f / %.15f  pseudo = %.15f  E(D,G) = %.15f  niter = %d"
           % (ecc, out["et_vikings"], out["et_tjl"], pseudo, out["E_from_densities"],
              len(energies) - 1))
 
 
-def gen_cfg2(pycc, solve=True, coupling="matched", name="cfg2.npz"):
+def gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz"):
     """no=20, nv=180, seed 1.  With the spec's plain sigma (coupling 1) CCSD diverges at this
     size, so the converged fixture uses the matched coupling; the raw-sigma fixture keeps the
     residual at the probe point only."""
-    no, nv, seed = CONFIGS[2]
+    no, nv, seed = WORKLOADS["o20v180"]
     fac = SyntheticFactors(no, nv, seed, coupling=coupling)
     t0 = time.time()
     F, ERI, L = fac.hamiltonian()
-    print("cfg2: integrals %.1f s" % (time.time() - t0), flush=True)
+    print("o20v180: integrals %.1f s" % (time.time() - t0), flush=True)
     w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
     o, v = w.o, w.v
     out = {"no": no, "nv": nv, "seed": seed, "B_checksum": float(np.sum(fac.B * fac.B)),
@@ -195,7 +195,7 @@ def gen_cfg2(pycc, solve=True, coupling="matched", name="cfg2.npz"):
     t1, t2 = probe_amplitudes(no, nv, w.t2, seed)
     t0 = time.time()
     r1, r2 = w.residuals(F, t1, t2)
-    print("cfg2: residual %.1f s" % (time.time() - t0), flush=True)
+    print("o20v180: residual %.1f s" % (time.time() - t0), flush=True)
     out["r1"] = r1
     out["r2_norm"] = float(np.linalg.norm(r2))
     out["r2_slice_ij01"] = r2[0, 1].copy()
@@ -214,27 +214,27 @@ def gen_cfg2(pycc, solve=True, coupling="matched", name="cfg2.npz"):
         w.cc_energy = rec
         t0 = time.time()
         ecc = quiet(w.solve_cc, 1e-10, 1e-10, 100, 8, 1)
-        print("cfg2: solve %.1f s, %d iterations" % (time.time() - t0, len(energies) - 1))
+        print("o20v180: solve %.1f s, %d iterations" % (time.time() - t0, len(energies) - 1))
         out["ecc"] = float(ecc)
         out["ecc_iters"] = np.array(energies)
         out["t1"] = w.t1
         out["t2_norm"] = float(np.linalg.norm(w.t2))
         out["t2_slice_ij01"] = w.t2[0, 1].copy()
     np.savez_compressed(os.path.join(HERE, name), **out)
-    print("cfg2: done", name, out.get("ecc"), flush=True)
+    print("o20v180: done", name, out.get("ecc"), flush=True)
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--cfg2", action="store_true")
-    ap.add_argument("--no-cfg1", action="store_true")
+    ap.add_argument("--o20v180", action="store_true")
+    ap.add_argument("--no-o5v19", action="store_true")
     args = ap.parse_args()
     pycc = import_reference()
-    if not args.no_cfg1:
-        gen_cfg1(pycc)
-    if args.cfg2:
-        gen_cfg2(pycc, solve=False, coupling=1.0, name="cfg2_raw.npz")
-        gen_cfg2(pycc, solve=True, coupling="matched", name="cfg2.npz")
+    if not args.no_o5v19:
+        gen_o5v19(pycc)
+    if args.o20v180:
+        gen_o20v180(pycc, solve=False, coupling=1.0, name="o20v180_raw.npz")
+        gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz")
 
 
 if __name__ == "__main__":

@@ -17,8 +17,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
-def adj1(cuda, cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def adj1(cuda, ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda))
     e = w.solve_cc(1e-12, 1e-12, 100)
     adj = CCSDAdjoint(w)
@@ -27,18 +27,18 @@ def adj1(cuda, cfg1_ham):
     return e, gF, Gam, adj
 
 
-def test_energy_identity(adj1, cfg1_ham, cuda):
+def test_energy_identity(adj1, ham_o5v19, cuda):
     e, gF, Gam, _ = adj1
-    _, F, ERI, _ = cfg1_ham
+    _, F, ERI, _ = ham_o5v19
     Ft, Et = torch.from_numpy(F).to(cuda), torch.from_numpy(ERI).to(cuda)
     lag = float((gF * Ft).sum() + (Gam * Et).sum())
     assert abs(lag - e) < 1e-10
 
 
-def test_densities_vs_reference(adj1, cfg1, cuda):
+def test_densities_vs_reference(adj1, golden_o5v19, cuda):
     _, gF, Gam, _ = adj1
-    D = torch.from_numpy(cfg1["D"]).to(cuda)
-    G = torch.from_numpy(cfg1["Gamma"]).to(cuda)
+    D = torch.from_numpy(golden_o5v19["D"]).to(cuda)
+    G = torch.from_numpy(golden_o5v19["Gamma"]).to(cuda)
     sym2 = lambda X: 0.5 * (X + X.T)
     assert (sym2(gF) - sym2(D)).abs().max().item() < 1e-9
     d = (symmetrize8(Gam) - symmetrize8(G)).abs().max().item()
@@ -62,9 +62,9 @@ def _energy(F, ERI, no, cuda):
     return w.solve_cc(1e-12, 1e-12, 200)
 
 
-def test_finite_differences(adj1, cfg1_ham, cuda):
+def test_finite_differences(adj1, ham_o5v19, cuda):
     _, gF, Gam, _ = adj1
-    _, F, ERI, _ = cfg1_ham
+    _, F, ERI, _ = ham_o5v19
     rng = np.random.default_rng(4)
     h = 1e-5
     gFn, Gn = gF.cpu().numpy(), Gam.cpu().numpy()
@@ -77,9 +77,9 @@ def test_finite_differences(adj1, cfg1_ham, cuda):
         assert abs(fd - an) < 1e-6 * max(abs(an), 1e-3), (fd, an)
 
 
-def test_autograd_function(adj1, cfg1_ham, cuda):
+def test_autograd_function(adj1, ham_o5v19, cuda):
     e, gF, Gam, _ = adj1
-    _, F, ERI, _ = cfg1_ham
+    _, F, ERI, _ = ham_o5v19
     Ft = torch.from_numpy(F).to(cuda).requires_grad_(True)
     Et = torch.from_numpy(ERI).to(cuda).requires_grad_(True)
     E = ccsd_energy(Ft, Et, 5, 1e-12, 1e-12)

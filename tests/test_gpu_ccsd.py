@@ -20,8 +20,8 @@ def rel(a, b):
 
 
 @pytest.fixture(scope="module")
-def wfn1(cuda, cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def wfn1(cuda, ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     H = pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda)
     return pg.CCwfn(H, device="GPU", precision="DP")
 
@@ -30,38 +30,38 @@ def dev(x, cuda):
     return torch.from_numpy(np.ascontiguousarray(x)).to(cuda)
 
 
-def test_mp2_guess(wfn1, cfg1):
+def test_mp2_guess(wfn1, golden_o5v19):
     e = float(wfn1.cc_energy(wfn1.o, wfn1.v, wfn1.H.F, wfn1.H.L, wfn1.t1, wfn1.t2))
-    assert abs(e - float(cfg1["ecc_mp2"])) < 1e-13
+    assert abs(e - float(golden_o5v19["ecc_mp2"])) < 1e-13
 
 
-def test_builders_cfg1(wfn1, cfg1, cuda):
+def test_builders_golden_o5v19(wfn1, golden_o5v19, cuda):
     w = wfn1
     o, v, F, ERI, L = w.o, w.v, w.H.F, w.H.ERI, w.H.L
-    t1, t2 = dev(cfg1["probe_t1"], cuda), dev(cfg1["probe_t2"], cuda)
-    assert rel(w.build_tau(t1, t2), cfg1["tau"]) < RTOL
-    assert rel(w.build_tau(t1, t2, 1.0, 0.5), cfg1["taut"]) < RTOL
-    assert rel(w.build_Fae(o, v, F, L, t1, t2), cfg1["Fae"]) < RTOL
-    assert rel(w.build_Fmi(o, v, F, L, t1, t2), cfg1["Fmi"]) < RTOL
-    assert rel(w.build_Fme(o, v, F, L, t1), cfg1["Fme"]) < RTOL
-    assert rel(w.build_Wmnij(o, v, ERI, t1, t2), cfg1["Wmnij"]) < RTOL
-    assert rel(w.build_Wmbej(o, v, ERI, L, t1, t2), cfg1["Wmbej"]) < RTOL
-    assert rel(w.build_Wmbje(o, v, ERI, t1, t2), cfg1["Wmbje"]) < RTOL
-    assert rel(w.build_Zmbij(o, v, ERI, t1, t2), cfg1["Zmbij"]) < RTOL
+    t1, t2 = dev(golden_o5v19["probe_t1"], cuda), dev(golden_o5v19["probe_t2"], cuda)
+    assert rel(w.build_tau(t1, t2), golden_o5v19["tau"]) < RTOL
+    assert rel(w.build_tau(t1, t2, 1.0, 0.5), golden_o5v19["taut"]) < RTOL
+    assert rel(w.build_Fae(o, v, F, L, t1, t2), golden_o5v19["Fae"]) < RTOL
+    assert rel(w.build_Fmi(o, v, F, L, t1, t2), golden_o5v19["Fmi"]) < RTOL
+    assert rel(w.build_Fme(o, v, F, L, t1), golden_o5v19["Fme"]) < RTOL
+    assert rel(w.build_Wmnij(o, v, ERI, t1, t2), golden_o5v19["Wmnij"]) < RTOL
+    assert rel(w.build_Wmbej(o, v, ERI, L, t1, t2), golden_o5v19["Wmbej"]) < RTOL
+    assert rel(w.build_Wmbje(o, v, ERI, t1, t2), golden_o5v19["Wmbje"]) < RTOL
+    assert rel(w.build_Zmbij(o, v, ERI, t1, t2), golden_o5v19["Zmbij"]) < RTOL
 
 
-def test_residuals_cfg1(wfn1, cfg1, cuda):
-    t1, t2 = dev(cfg1["probe_t1"], cuda), dev(cfg1["probe_t2"], cuda)
+def test_residuals_golden_o5v19(wfn1, golden_o5v19, cuda):
+    t1, t2 = dev(golden_o5v19["probe_t1"], cuda), dev(golden_o5v19["probe_t2"], cuda)
     r1, r2 = wfn1.residuals(wfn1.H.F, t1, t2)
-    assert rel(r1, cfg1["r1"]) < RTOL
-    assert rel(r2, cfg1["r2"]) < RTOL
+    assert rel(r1, golden_o5v19["r1"]) < RTOL
+    assert rel(r2, golden_o5v19["r2"]) < RTOL
     e = float(wfn1.cc_energy(wfn1.o, wfn1.v, wfn1.H.F, wfn1.H.L, t1, t2))
-    assert abs(e - float(cfg1["ecc_probe"])) < 1e-13
+    assert abs(e - float(golden_o5v19["ecc_probe"])) < 1e-13
 
 
-def test_residual_vs_oracle_random_point(cuda, cfg1_ham):
+def test_residual_vs_oracle_random_point(cuda, ham_o5v19):
     """A fresh seeded point (not in the fixtures): GPU FP64 vs the numpy oracle."""
-    _, F, ERI, L = cfg1_ham
+    _, F, ERI, L = ham_o5v19
     rng = np.random.default_rng(99)
     t1 = 0.05 * rng.standard_normal((5, 19))
     t2 = 0.05 * rng.standard_normal((5, 5, 19, 19))
@@ -73,25 +73,25 @@ def test_residual_vs_oracle_random_point(cuda, cfg1_ham):
     assert rel(r1, r1o) < RTOL and rel(r2, r2o) < RTOL
 
 
-def test_solve_cc_cfg1(cuda, cfg1_ham, cfg1):
-    _, F, ERI, L = cfg1_ham
+def test_solve_cc_golden_o5v19(cuda, ham_o5v19, golden_o5v19):
+    _, F, ERI, L = ham_o5v19
     w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda))
     e = w.solve_cc(1e-12, 1e-12, 100)
-    assert abs(e - float(cfg1["ecc"])) < 1e-10
-    assert len(w.energies) == len(cfg1["ecc_iters"])
-    assert np.abs(np.array(w.energies) - cfg1["ecc_iters"]).max() < 1e-10
-    assert rel(w.t2, cfg1["t2"]) < 1e-8
+    assert abs(e - float(golden_o5v19["ecc"])) < 1e-10
+    assert len(w.energies) == len(golden_o5v19["ecc_iters"])
+    assert np.abs(np.array(w.energies) - golden_o5v19["ecc_iters"]).max() < 1e-10
+    assert rel(w.t2, golden_o5v19["t2"]) < 1e-8
 
 
-def test_solve_cc_raises_on_maxiter(cuda, cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def test_solve_cc_raises_on_maxiter(cuda, ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda))
     with pytest.raises(pg.ConvergenceError):
         w.solve_cc(1e-14, 1e-14, maxiter=3)
 
 
-def test_gpu_built_blocks_match_host(cuda, cfg1_ham):
-    fac, F, ERI, L = cfg1_ham
+def test_gpu_built_blocks_match_host(cuda, ham_o5v19):
+    fac, F, ERI, L = ham_o5v19
     Hg = pg.Hamiltonian.from_factors(fac, device=cuda)
     Hh = pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda)
     for pat, blk in Hh.ERI.blocks.items():
@@ -124,15 +124,15 @@ def _probe(no, nv, t2_mp2, seed):
 
 
 @pytest.fixture(scope="module")
-def cfg2_data():
+def golden_o20v180_data():
     from conftest import golden
-    return golden("cfg2.npz"), golden("cfg2_raw.npz")
+    return golden("o20v180.npz"), golden("o20v180_raw.npz")
 
 
 @pytest.mark.parametrize("which", ["matched", "raw"])
-def test_residual_cfg2_vs_reference(cuda, cfg2_data, which):
+def test_residual_o20v180_vs_reference(cuda, golden_o20v180_data, which):
     """no=20, nv=180: GPU FP64 residual against the reference's own output (both couplings)."""
-    g = cfg2_data[0] if which == "matched" else cfg2_data[1]
+    g = golden_o20v180_data[0] if which == "matched" else golden_o20v180_data[1]
     fac = pg.SyntheticFactors(20, 180, 1, coupling="matched" if which == "matched" else 1.0)
     H = pg.Hamiltonian.from_factors(fac, device=cuda)
     w = pg.CCwfn(H)
@@ -146,9 +146,9 @@ def test_residual_cfg2_vs_reference(cuda, cfg2_data, which):
     assert abs(np.linalg.norm(r2) - float(g["r2_norm"])) < RTOL * float(g["r2_norm"])
 
 
-def test_solve_cfg2_vs_reference(cuda, cfg2_data):
+def test_solve_o20v180_vs_reference(cuda, golden_o20v180_data):
     """Converged FP64 GPU energy within 1e-10 Eh of the reference's at no=20, nv=180."""
-    g = cfg2_data[0]
+    g = golden_o20v180_data[0]
     H = pg.Hamiltonian.from_factors(pg.SyntheticFactors(20, 180, 1, coupling="matched"), device=cuda)
     w = pg.CCwfn(H)
     e = w.solve_cc(1e-10, 1e-10, 100)

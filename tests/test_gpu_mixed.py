@@ -144,36 +144,36 @@ def test_split_k_small_output(cuda):
 
 
 @pytest.fixture(scope="module")
-def h1(cuda, cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def h1(cuda, ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     return pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda)
 
 
-def test_mixed_residual_cfg1(cuda, h1, cfg1):
-    t1 = torch.from_numpy(cfg1["probe_t1"]).to(cuda)
-    t2 = torch.from_numpy(np.ascontiguousarray(cfg1["probe_t2"])).to(cuda)
+def test_mixed_residual_golden_o5v19(cuda, h1, golden_o5v19):
+    t1 = torch.from_numpy(golden_o5v19["probe_t1"]).to(cuda)
+    t2 = torch.from_numpy(np.ascontiguousarray(golden_o5v19["probe_t2"])).to(cuda)
     for mode, tol in (("bf16x3", 1e-4), ("fast", 5e-2)):
         w = pg.CCwfn(h1, precision="MIXED")
         w.mixed_engine().select_mode(0.0 if mode == "bf16x3" else 1.0)
         r1, r2 = w.residuals(h1.F, t1, t2)
         torch.cuda.synchronize()
-        e1 = np.abs(r1.cpu().numpy() - cfg1["r1"]).max() / np.abs(cfg1["r1"]).max()
-        e2 = np.abs(r2.cpu().numpy() - cfg1["r2"]).max() / np.abs(cfg1["r2"]).max()
+        e1 = np.abs(r1.cpu().numpy() - golden_o5v19["r1"]).max() / np.abs(golden_o5v19["r1"]).max()
+        e2 = np.abs(r2.cpu().numpy() - golden_o5v19["r2"]).max() / np.abs(golden_o5v19["r2"]).max()
         assert e1 < tol and e2 < tol, (mode, e1, e2)
 
 
-def test_mixed_solve_cfg1(cuda, h1, cfg1):
+def test_mixed_solve_golden_o5v19(cuda, h1, golden_o5v19):
     w = pg.CCwfn(h1, precision="MIXED")
     e = w.solve_cc(1e-9, 1e-7, 100)
-    assert abs(e - float(cfg1["ecc"])) < 1e-6
+    assert abs(e - float(golden_o5v19["ecc"])) < 1e-6
     assert w.mixed_engine().is_final_mode()
 
 
-def test_sp_solve_cfg1(cuda, h1, cfg1):
+def test_sp_solve_golden_o5v19(cuda, h1, golden_o5v19):
     """precision='SP' (split-BF16x3 throughout) within 1e-7 of DP, as the reference's SP test."""
     w = pg.CCwfn(h1, precision="SP")
     e = w.solve_cc(1e-9, 1e-7, 100)
-    assert abs(e - float(cfg1["ecc"])) < 1e-7
+    assert abs(e - float(golden_o5v19["ecc"])) < 1e-7
 
 
 @pytest.mark.parametrize("no,nv", [(3, 17), (7, 33)])

@@ -21,23 +21,23 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.fixture(scope="module")
-def w1(cuda, cfg1_ham, cfg1):
-    _, F, ERI, L = cfg1_ham
+def w1(cuda, ham_o5v19, golden_o5v19):
+    _, F, ERI, L = ham_o5v19
     w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda))
-    w.t1.copy_(torch.from_numpy(cfg1["t1"]))
-    w.t2.copy_(torch.from_numpy(np.ascontiguousarray(cfg1["t2"])))
+    w.t1.copy_(torch.from_numpy(golden_o5v19["t1"]))
+    w.t2.copy_(torch.from_numpy(np.ascontiguousarray(golden_o5v19["t2"])))
     return w
 
 
-def test_fp64_triples_cfg1(w1, cfg1):
+def test_fp64_triples_golden_o5v19(w1, golden_o5v19):
     et = t_energy_fp64(w1)
-    assert abs(et - float(cfg1["et_tjl"])) < 1e-11
-    assert abs(et - float(cfg1["et_vikings"])) < 1e-11
+    assert abs(et - float(golden_o5v19["et_tjl"])) < 1e-11
+    assert abs(et - float(golden_o5v19["et_vikings"])) < 1e-11
 
 
-def test_tc_triples_cfg1(w1, cfg1):
+def test_tc_triples_golden_o5v19(w1, golden_o5v19):
     et = t_energy_tc(w1, batch=7)
-    ref = float(cfg1["et_tjl"])
+    ref = float(golden_o5v19["et_tjl"])
     assert abs(et - ref) < 2e-3 * abs(ref), (et, ref)
 
 
@@ -57,11 +57,11 @@ def test_triples_vs_oracle(cuda, no, nv):
     assert abs(et_tc - ref) < 2e-3 * abs(ref)
 
 
-def test_ccsd_t_model(cuda, cfg1_ham, cfg1):
-    _, F, ERI, L = cfg1_ham
+def test_ccsd_t_model(cuda, ham_o5v19, golden_o5v19):
+    _, F, ERI, L = ham_o5v19
     w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda), model="CCSD(T)")
     e = w.solve_cc(1e-12, 1e-12, 100)
-    assert abs(e - (float(cfg1["ecc"]) + float(cfg1["et_tjl"]))) < 1e-10
+    assert abs(e - (float(golden_o5v19["ecc"]) + float(golden_o5v19["et_tjl"]))) < 1e-10
 
 
 @pytest.mark.parametrize("layout", ["row", "col"])

@@ -10,48 +10,48 @@ def rel(a, b):
     return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
 
 
-def test_generator_matches_golden(cfg1, cfg1_ham):
-    fac = cfg1_ham[0]
-    assert float(np.sum(fac.B * fac.B)) == pytest.approx(float(cfg1["B_checksum"]), rel=1e-14)
-    assert np.array_equal(fac.eps, cfg1["eps"])
+def test_generator_matches_golden(golden_o5v19, ham_o5v19):
+    fac = ham_o5v19[0]
+    assert float(np.sum(fac.B * fac.B)) == pytest.approx(float(golden_o5v19["B_checksum"]), rel=1e-14)
+    assert np.array_equal(fac.eps, golden_o5v19["eps"])
 
 
-def test_intermediates_cfg1(cfg1, cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def test_intermediates_golden_o5v19(golden_o5v19, ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     o, v = slice(0, 5), slice(5, 24)
-    X = oc.intermediates(o, v, F, ERI, L, cfg1["probe_t1"], cfg1["probe_t2"])
+    X = oc.intermediates(o, v, F, ERI, L, golden_o5v19["probe_t1"], golden_o5v19["probe_t2"])
     for k, val in X.items():
-        assert rel(val, cfg1[k]) < 1e-13, k
-    assert rel(oc.build_tau(cfg1["probe_t1"], cfg1["probe_t2"]), cfg1["tau"]) < 1e-14
-    assert rel(oc.build_tau(cfg1["probe_t1"], cfg1["probe_t2"], 1.0, 0.5), cfg1["taut"]) < 1e-14
+        assert rel(val, golden_o5v19[k]) < 1e-13, k
+    assert rel(oc.build_tau(golden_o5v19["probe_t1"], golden_o5v19["probe_t2"]), golden_o5v19["tau"]) < 1e-14
+    assert rel(oc.build_tau(golden_o5v19["probe_t1"], golden_o5v19["probe_t2"], 1.0, 0.5), golden_o5v19["taut"]) < 1e-14
 
 
-def test_residuals_cfg1(cfg1, cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def test_residuals_golden_o5v19(golden_o5v19, ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     o, v = slice(0, 5), slice(5, 24)
-    r1, r2 = oc.residuals(o, v, F, ERI, L, cfg1["probe_t1"], cfg1["probe_t2"])
-    assert rel(r1, cfg1["r1"]) < 1e-12
-    assert rel(r2, cfg1["r2"]) < 1e-12
+    r1, r2 = oc.residuals(o, v, F, ERI, L, golden_o5v19["probe_t1"], golden_o5v19["probe_t2"])
+    assert rel(r1, golden_o5v19["r1"]) < 1e-12
+    assert rel(r2, golden_o5v19["r2"]) < 1e-12
     t1, t2 = oc.mp2_guess(F, ERI, 5)
     r1, r2 = oc.residuals(o, v, F, ERI, L, t1, t2)
-    assert rel(r2, cfg1["r2_mp2"]) < 1e-12
-    assert np.abs(r1 - cfg1["r1_mp2"]).max() < 1e-14
-    assert oc.cc_energy(o, v, F, L, t1, t2) == pytest.approx(float(cfg1["ecc_mp2"]), abs=1e-14)
-    assert oc.cc_energy(o, v, F, L, cfg1["probe_t1"], cfg1["probe_t2"]) == pytest.approx(
-        float(cfg1["ecc_probe"]), abs=1e-13)
+    assert rel(r2, golden_o5v19["r2_mp2"]) < 1e-12
+    assert np.abs(r1 - golden_o5v19["r1_mp2"]).max() < 1e-14
+    assert oc.cc_energy(o, v, F, L, t1, t2) == pytest.approx(float(golden_o5v19["ecc_mp2"]), abs=1e-14)
+    assert oc.cc_energy(o, v, F, L, golden_o5v19["probe_t1"], golden_o5v19["probe_t2"]) == pytest.approx(
+        float(golden_o5v19["ecc_probe"]), abs=1e-13)
 
 
-def test_solve_cc_cfg1(cfg1, cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def test_solve_cc_golden_o5v19(golden_o5v19, ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     e, t1, t2, es = oc.solve_cc(F, ERI, L, 5, 1e-12, 1e-12)
-    assert abs(e - float(cfg1["ecc"])) < 1e-11
-    assert len(es) == len(cfg1["ecc_iters"])
-    assert np.abs(np.array(es) - cfg1["ecc_iters"]).max() < 1e-11
-    assert rel(t2, cfg1["t2"]) < 1e-9
+    assert abs(e - float(golden_o5v19["ecc"])) < 1e-11
+    assert len(es) == len(golden_o5v19["ecc_iters"])
+    assert np.abs(np.array(es) - golden_o5v19["ecc_iters"]).max() < 1e-11
+    assert rel(t2, golden_o5v19["t2"]) < 1e-9
 
 
-def test_solve_cc_raises_on_maxiter(cfg1_ham):
-    _, F, ERI, L = cfg1_ham
+def test_solve_cc_raises_on_maxiter(ham_o5v19):
+    _, F, ERI, L = ham_o5v19
     with pytest.raises(RuntimeError):
         oc.solve_cc(F, ERI, L, 5, 1e-14, 1e-14, maxiter=3)
 
@@ -64,18 +64,18 @@ def probe_amplitudes(no, nv, t2_mp2, seed):
     return t1, t2_mp2 + noise + noise.transpose(1, 0, 3, 2)
 
 
-def test_generator_cfg2_checksums():
+def test_generator_o20v180_checksums():
     from conftest import golden
-    for name, coupling in (("cfg2.npz", "matched"), ("cfg2_raw.npz", 1.0)):
+    for name, coupling in (("o20v180.npz", "matched"), ("o20v180_raw.npz", 1.0)):
         g = golden(name)
         fac = SyntheticFactors(20, 180, 1, coupling=coupling)
         assert float(np.sum(fac.B * fac.B)) == pytest.approx(float(g["B_checksum"]), rel=1e-13)
 
 
-def test_residuals_cfg2_golden():
+def test_residuals_o20v180_golden():
     """The oracle's residual at no=20, nv=180 against the reference's (about a minute)."""
     from conftest import golden
-    g = golden("cfg2.npz")
+    g = golden("o20v180.npz")
     fac = SyntheticFactors(20, 180, 1, coupling="matched")
     F, ERI, L = fac.hamiltonian()
     o, v = slice(0, 20), slice(20, 200)
