@@ -516,20 +516,25 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
   const int fx = tid % NF, w0 = tid / NF;
   const bool fx_ok = KF ? (k0 + fx < p.K) : (r0 + fx < p.R);
   const long long wlim = KF ? (p.R - r0) : (p.K - k0);
-  long long f[4];
-#pragma unroll
-  for (int s = 0; s < 4; ++s) f[s] = KF ? t.kof[s][fx] : t.rof[s][fx];
+  long long f[4] = {0, 0, 0, 0};
+  if (p.X) f[0] = KF ? t.kof[0][fx] : t.rof[0][fx];
+  if (p.Y) f[1] = KF ? t.kof[1][fx] : t.rof[1][fx];
+  if (p.P) {
+    f[2] = KF ? t.kof[2][fx] : t.rof[2][fx];
+    f[3] = KF ? t.kof[3][fx] : t.rof[3][fx];
+  }
   V vals[PER];
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
     const int wv = w0 + u * STEP;
     V v = 0;
     if (fx_ok && wv < wlim) {
-      const long long w[4] = {KF ? t.rof[0][wv] : t.kof[0][wv], KF ? t.rof[1][wv] : t.kof[1][wv],
-                              KF ? t.rof[2][wv] : t.kof[2][wv], KF ? t.rof[3][wv] : t.kof[3][wv]};
-      if (p.X) v = a * pack_ld<V>(p.X + f[0] + w[0]);
-      if (p.Y) v += b * pack_ld<V>(p.Y + f[1] + w[1]);
-      if (p.P) v += c * pack_ld<V>(p.P + f[2] + w[2]) * pack_ld<V>(p.Q + f[3] + w[3]);
+      // each source's walked offset is read inside its (block-uniform) branch, so an
+      // operand with X alone reads one offset per element
+      auto wof = [&](int src) { return KF ? t.rof[src][wv] : t.kof[src][wv]; };
+      if (p.X) v = a * pack_ld<V>(p.X + f[0] + wof(0));
+      if (p.Y) v += b * pack_ld<V>(p.Y + f[1] + wof(1));
+      if (p.P) v += c * pack_ld<V>(p.P + f[2] + wof(2)) * pack_ld<V>(p.Q + f[3] + wof(3));
     }
     vals[u] = v;
   }

@@ -1,0 +1,116 @@
+"""Host logic of the tensor-core engine, on CPU with the pack and GEMM launches recorded
+instead of run: the GEMM orientation (the output's unit-stride index on the 128-row side),
+the K order, the caches of packed operands and the precision ladder's release of packed
+integrals no later stage reads.
+"""
+import pytest
+import torch
+
+import pycc_gb300.tc as tc
+from pycc_gb300.tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X6, FMT_FP8, Operand,
+                           Packed, TCEngine, static_pack_format)
+
+
+@pytest.fixture
+def recorder(monkeypatch):
+    calls = {"pack": [], "gemm": []}
+
+    def fake_pack(op, rows, ks, fmt, stream=None, row_tab=None):
+        ext = op.extents()
+        R = 1
+        for c in rows:
+            R *= ext[c]
+        calls["pack"].append((op.labels, tuple(rows), tuple(ks), fmt, op.key))
+        return Packed(fmt, R, 64, None)
+
+    def fake_gemm(fmt, A, B, out, rows, cols, rhs, **kw):
+        calls["gemm"].append((fmt, A.rows, B.rows, tuple(rows), tuple(cols), rhs))
+
+    monkeypatch.setattr(tc, "pack", fake_pack)
+    monkeypatch.setattr(tc, "gemm", fake_gemm)
+    return calls
+
+
+def t(*shape):
+    return torch.zeros(shape, dtype=torch.float64)
+
+
+def test_orientation_follows_output_unit_stride(recorder):
+    """The operand holding the output's unit-stride index supplies the 128-row side (a
+    warp's 32 rows are then 32 consecutive output addresses), unless that side is shorter
+    than one 128-row tile."""
+    eng = TCEngine("cpu")
+    # mbej, j unit-stride and j held by t1: 200 occupied orbitals fill the rows
+    o, v = 200, 3
+    eng.contract("jf,mbef->mbej", Operand.of("jf", t(o, v)), Operand.of("mbef", t(o, v, v, v)),
+                 t(o, v, v, o))
+    fmt, M, N, rows, cols, rhs = recorder["gemm"][-1]
+    assert rows == ("j",) and M == o and cols == ("m", "b", "e")
+    # the same term with 4 occupied orbitals: j is too short, (m, b, e) takes the rows
+    o, v = 4, 300
+    eng.contract("jf,mbef->mbej", Operand.of("jf", t(o, v)), Operand.of("mbef", t(o, v, v, v)),
+                 t(o, v, v, o))
+    fmt, M, N, rows, cols, rhs = recorder["gemm"][-1]
+    assert rows == ("m", "b", "e") and M == o * v * v and cols == ("j",)
+    # ijab, b unit-stride and held by F_be (300 rows)
+    eng.contract("ijae,be->ijab", Operand.of("ijae", t(o, o, v, v)), Operand.of("be", t(v, v)),
+                 t(o, o, v, v))
+    fmt, M, N, rows, cols, rhs = recorder["gemm"][-1]
+    assert rows == ("b",) and M == v and cols == ("i", "j", "a")
+
+
+def test_k_order_follows_dynamic_operand_strides(recorder):
+    """K is ordered by the dynamic operand's strides, slowest first, so its gather runs
+    along its own memory order."""
+    o, v = 3, 5
+    eng = TCEngine("cpu")
+    t2 = t(o, o, v, v)
+    L = Operand.of("mnef", t(o, o, v, v), key=("L", "oovv"))
+    eng.contract("inef,mnef->mi", Operand.of("inef", t2), L, t(o, o))
+    ks = [c[2] for c in recorder["pack"]]
+    assert all(k == ("n", "e", "f") for k in ks)
+
+
+def test_static_and_dynamic_caches(recorder):
+    """Static operands are packed once per (block, labels, layout, pieces) and BF16 GEMMs
+    reuse the split-BF16x3 pack; dynamic operands are packed once per residual."""
+    o, v = 3, 5
+    eng = TCEngine("cpu")
+    V = Operand.of("mbef", t(o, v, v, v), key=("ERI", "ovvv"))
+    t1 = t(o, v)
+    for fmt in (FMT_BF16, FMT_BF16X3F, FMT_BF16X3, FMT_BF16):
+        eng.contract("jf,mbef->mbej", Operand.of("jf", t1), V, t(o, v, v, o), fmt=fmt)
+    static = [c for c in recorder["pack"] if c[4] is not None]
+    assert len(static) == 1 and static[0][3] == FMT_BF16X3
+    assert len(eng.cache) == 1
+    eng.dyn_cache = {}
+    n0 = len(recorder["pack"])
+    for _ in range(3):
+        eng.contract("jf,mbef->mbej", Operand.of("jf", t1), V, t(o, v, v, o), fmt=FMT_BF16X3)
+    assert len(recorder["pack"]) == n0 + 1                # t1 packed once per residual
+
+
+def test_static_pack_formats():
+    assert static_pack_format(FMT_BF16) == FMT_BF16X3
+    assert static_pack_format(FMT_BF16X3F) == FMT_BF16X3
+    assert static_pack_format(FMT_BF16X3) == FMT_BF16X3
+    assert static_pack_format(FMT_FP8) == FMT_FP8
+    assert static_pack_format(FMT_BF16X6) == FMT_BF16X6
+
+
+def test_ladder_prunes_formats_no_later_stage_reads():
+    """Advancing the precision ladder frees the packed integrals of formats that no later
+    stage reads (the FP8 ladder operand after the FP8 stage)."""
+    from pycc_gb300.mixed import MixedResidual
+
+    class W:
+        device1, stream, vvvv_fp8, switch_threshold = "cpu", None, True, 1e-5
+
+    m = MixedResidual(W())
+    assert m.stages == ["fp8", "bf16", "bf16x3f", "bf16x3"]
+    m.tc.cache = {("ERI", "vvvv", FMT_FP8): 1, ("ERI", "ovvv", FMT_BF16X3): 2}
+    m._advance()                                         # fp8 -> bf16
+    assert list(m.tc.cache) == [("ERI", "ovvv", FMT_BF16X3)]
+    m._advance()
+    m._advance()                                         # split stages keep the pack
+    assert list(m.tc.cache) == [("ERI", "ovvv", FMT_BF16X3)]
