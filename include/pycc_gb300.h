@@ -186,7 +186,8 @@ int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* 
  *   products of order <= 2^-16 (smallest first), 2 = FP8 with the row scales applied in the
  *   epilogue.  off_m / off_n: flat index over up to 4 sub-indices (extents, element strides
  *   in C); col_map (optional, device, N entries) replaces off_n and col_scale (optional,
- *   device, N doubles) multiplies each column.  status: device int, set non-zero when a
+ *   device, N doubles) multiplies each column.  Column offsets (off_n or col_map) lie in
+ *   [0, 2^31); row offsets are 64-bit.  status: device int, set non-zero when a
  *   bounded device-side wait expired (the kernel then skips its stores). */
 int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, long long M,
                 long long lda, const void* B_hi, const void* B_mid, const void* B_lo, long long N,

@@ -101,7 +101,7 @@ struct Smem {
   static constexpr int B_BYTES = BN * KBYTES;
   static constexpr int STAGE = NP * (A_BYTES + B_BYTES);
   // barriers / tmem slot / flags, then per epilogue warp BN/2 column offsets and scales
-  static constexpr int TAIL = 512 + GEMM_EPI_WARPS * (BN / 2) * 12;
+  static constexpr int TAIL = 512 + GEMM_EPI_WARPS * (BN / 2) * 8;
   static constexpr int FIT = (kSmemMax - 1024 - TAIL) / STAGE;
   static constexpr int STAGES = FIT > 8 ? 8 : FIT;
   static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
@@ -135,26 +135,27 @@ __device__ __forceinline__ int epi_col(int h, int jj) {
   return 32 * (NB - 1) + 16 * h + (jj - 32 * NFULL);
 }
 
+// Column offsets are 32-bit (the host checks that every column offset of C is below 2^31;
+// the row offset stays 64-bit), so a batch's offsets stay in registers next to its
+// accumulator values and old C values.
 template <int W>
-__device__ __forceinline__ void epi_batch(uint32_t taddr, const long long* co, const float* sc,
+__device__ __forceinline__ void epi_batch(uint32_t taddr, const int* co, const float* sc,
                                           bool row_ok, double* crow, float ascale,
                                           double cscale, bool need_old, int atomic_out) {
   uint32_t r[W];
   if constexpr (W == 32) tmem_ld32(taddr, r);
   else tmem_ld16(taddr, r);
   if (!row_ok) return;
+  int cj[W];
   double old[W];
 #pragma unroll
   for (int j = 0; j < W; ++j) {
-    const long long c = co[j];
-    old[j] = (need_old && c >= 0) ? crow[c] : 0.0;
+    cj[j] = co[j];
+    old[j] = (need_old && cj[j] >= 0) ? crow[cj[j]] : 0.0;
   }
-  // the offsets are read again from shared memory rather than held in registers across
-  // the loads (r and old already take 3 W of the thread's registers)
-  const volatile long long* cov = co;
 #pragma unroll
   for (int j = 0; j < W; ++j) {
-    const long long c = cov[j];
+    const int c = cj[j];
     if (c < 0) continue;
     const double v = f32_to_f64(__uint_as_float(r[j]) * (ascale * sc[j]));
     if (atomic_out)
@@ -192,8 +193,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   constexpr int HB = BN / 2;  // columns drained by one epilogue warp
-  long long* colofs_all = reinterpret_cast<long long*>(tail + 512);  // [8 warps][HB]
-  float* colsc_all = reinterpret_cast<float*>(tail + 512 + GEMM_EPI_WARPS * HB * 8);
+  int* colofs_all = reinterpret_cast<int*>(tail + 512);  // [8 warps][HB]
+  float* colsc_all = reinterpret_cast<float*>(tail + 512 + GEMM_EPI_WARPS * HB * 4);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long ntiles = p.mt * p.nt * p.splits;
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
     // ---- epilogue warps: TMEM -> registers -> FP64 C, one chunk at a time ----
     const int q = warp & 3;         // the TMEM lane quarter this warp may read
     const int h = (warp - 2) >> 2;  // the half of the tile's columns it drains
-    long long* colofs = colofs_all + (warp - 2) * HB;
+    int* colofs = colofs_all + (warp - 2) * HB;
     float* colsc = colsc_all + (warp - 2) * HB;
     int u = 0;
     bool stop = false;
@@ -366,7 +367,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       for (int j = lane; j < HB; j += 32) {
         const long long c = n0 + epi_col<BN>(h, j);
         const bool in = c < p.N;
-        colofs[j] = in ? (p.col_map ? p.col_map[c] : epi_offset(p.en, c)) : -1;
+        colofs[j] = in ? (int)(p.col_map ? p.col_map[c] : epi_offset(p.en, c)) : -1;
         double sc = p.alpha;
         if (in && p.fp8) sc *= (double)p.b_scale[c];
         if (in && p.col_scale) sc *= p.col_scale[c];
@@ -900,6 +901,14 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.pt = (fmt == kBF16x3) ? t3 : (fmt == kBF16x6 ? t6 : t1);
   a.npass = a.pt.n;
   if (!fill_epi(a.em, m_n, m_ext, m_sc, "M") || !fill_epi(a.en, n_n, n_ext, n_sc, "N")) return -1;
+  if (!col_map) {  // the epilogue keeps column offsets in 32 bits
+    long long span = 0;
+    for (int q = 0; q < a.en.n; ++q) span += (a.en.ext[q] - 1) * llabs(a.en.s[q]);
+    if (span > 0x7fffffffLL) {
+      set_error("pcg_tc_gemm: column offsets of C reach %lld (limit 2^31 - 1)", span);
+      return -1;
+    }
+  }
   a.alpha = alpha;
   a.beta = beta;
   a.C = C;
