@@ -340,7 +340,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-terms", action="store_true")
-    ap.add_argument("--force-mode", default=None, choices=[None, "bf16x3f", "bf16x3"],
+    ap.add_argument("--force-mode", default=None, choices=[None, "bf16x3f", "bf16x3s", "bf16x3"],
                     help="run every iteration in this precision stage (profiling of that stage)")
     ap.add_argument("--converge-iters", type=int, default=60,
                     help="untimed iterations allowed after the timed ones to reach the floor")
@@ -449,7 +449,7 @@ def main():
     roofline = None
     if ladder:
         lr = ladder[0]
-        npass = {0: 1, 1: 3, 2: 1, 3: 6, 4: 3}[lr["fmt"]]
+        npass = {0: 1, 1: 3, 2: 1, 3: 6, 4: 3, 5: 3}[lr["fmt"]]
         pairs = o_n * (o_n + 1) // 2
         # algorithmic work of the launch: the reference's ladder term, 2 o^2 v^4 flop
         alg = 2.0 * o_n**2 * v_n**4
@@ -466,7 +466,8 @@ def main():
                     "unit": "TFLOP/s", "frac": achieved / pk["bf16"], "traffic": traffic,
                     "traffic_unit": "bytes per launch (ncu capture)" if traffic else None,
                     "kernel": "tc_gemm_kernel ladder ijef,abef->ijab (i<=j pairs)",
-                    "mode": {0: "bf16", 1: "bf16x3", 2: "fp8", 3: "bf16x6", 4: "bf16x3f"}[lr["fmt"]],
+                    "mode": {0: "bf16", 1: "bf16x3", 2: "fp8", 3: "bf16x6", 4: "bf16x3f",
+                             5: "bf16x3s"}[lr["fmt"]],
                     "algorithmic_flop_per_launch": alg, "executed_flop_per_launch": work,
                     "passes": npass, "executed_tflops": executed,
                     "executed_frac": executed / pk["bf16"],

@@ -182,6 +182,9 @@ int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* 
  *   A: M rows of lda elements (K-major, 16-byte aligned rows), B: N rows of ldb elements;
  *   format as above, plus 4 = split-BF16x3 fused (both pieces of A and B loaded per stage,
  *   the three products issued from it; faster, with a slightly larger FP32 truncation bias),
+ *   5 = split-BF16x3 fused with the small products and the leading product in separate
+ *   FP32 accumulators added once per chunk (the accuracy of 1, the traffic of 4; N tiles
+ *   of at most 128 columns),
  *   1 = three tcgen05 passes Al.Bh + Ah.Bl + Ah.Bh, 3 = the six piece
  *   products of order <= 2^-16 (smallest first), 2 = FP8 with the row scales applied in the
  *   epilogue.  off_m / off_n: flat index over up to 4 sub-indices (extents, element strides

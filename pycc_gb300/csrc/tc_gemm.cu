@@ -7,8 +7,10 @@
 //   (index permutations, the tau / 2t2-t2' combinations and the t1 outer products are
 //   folded into the gather, together with the precision conversion).
 // * Formats: BF16; split-BF16x3 (A = Ah + Al, B = Bh + Bl, three passes Ah.Bh + Ah.Bl +
-//   Al.Bh accumulated in the same TMEM tile); FP8 E4M3 with one FP32 scale per row of
-//   each operand (applied in the epilogue).
+//   Al.Bh accumulated in the same TMEM tile), fused (all three products from one stage)
+//   and fused with separate accumulators for the small and the leading products;
+//   split-BF16x6; FP8 E4M3 with one FP32 scale per row of each operand (applied in the
+//   epilogue).
 // * Mainloop: one CTA computes a 128 x BN FP32 tile in TMEM.  Warp 0 lane 0 issues TMA
 //   (cp.async.bulk.tensor, 128B swizzle) into an S-stage shared-memory ring; warp 1
 //   lane 0 issues tcgen05.mma (kind::f16 or kind::f8f6f4) and releases stages with
@@ -25,7 +27,7 @@
 namespace pcg {
 namespace tc {
 
-enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2, kBF16x6 = 3, kBF16x3F = 4 };
+enum Fmt : int { kBF16 = 0, kBF16x3 = 1, kFP8 = 2, kBF16x6 = 3, kBF16x3F = 4, kBF16x3S = 5 };
 
 // Operand pieces multiplied in each pass (A piece, B piece), smallest products first so
 // the FP32 accumulator sums the small corrections before the leading term.
@@ -95,7 +97,12 @@ constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI_WARPS;
 // NP operand pieces per stage: 1 (one product per stage; split formats run one pass per
 // product), or 2 (split-BF16x3 with both pieces of A and B in the stage, all three products
 // issued from it: a third less shared-memory fill traffic per flop).
-template <int BN, int NP = 1>
+// SPLIT (fused split-BF16x3 only): the two small products Al.Bh + Ah.Bl accumulate in a
+// TMEM accumulator of their own, the leading Ah.Bh in another, and the epilogue adds them
+// once.  The small corrections then never meet the leading term's magnitude inside the
+// truncating FP32 accumulator (the by-pass format's accuracy, at the fused format's
+// traffic); four BN-column accumulators (two buffers) limit BN to 128.
+template <int BN, int NP = 1, bool SPLIT = false>
 struct Smem {
   static constexpr int A_BYTES = BM * KBYTES;
   static constexpr int B_BYTES = BN * KBYTES;
@@ -105,8 +112,10 @@ struct Smem {
   static constexpr int FIT = (kSmemMax - 1024 - TAIL) / STAGE;
   static constexpr int STAGES = FIT > 8 ? 8 : FIT;
   static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
-  static constexpr unsigned TMEM_COLS = (2 * BN <= 128) ? 128 : ((2 * BN <= 256) ? 256 : 512);
+  static constexpr int ACC = SPLIT ? 2 * BN : BN;  // TMEM columns of one buffer
+  static constexpr unsigned TMEM_COLS = (2 * ACC <= 128) ? 128 : ((2 * ACC <= 256) ? 256 : 512);
   static_assert(BN % 32 == 0 && BN >= 64 && BN <= 256, "BN: multiple of 32 in [64, 256]");
+  static_assert(2 * ACC <= 512 && (!SPLIT || NP == 2), "TMEM holds 512 columns");
   static_assert(STAGES >= 2, "shared-memory ring too shallow");
 };
 
@@ -138,13 +147,22 @@ __device__ __forceinline__ int epi_col(int h, int jj) {
 // Column offsets are 32-bit (the host checks that every column offset of C is below 2^31;
 // the row offset stays 64-bit), so a batch's offsets stay in registers next to its
 // accumulator values and old C values.
-template <int W>
+template <int W, bool SPLIT = false>
 __device__ __forceinline__ void epi_batch(uint32_t taddr, const int* co, const float* sc,
                                           bool row_ok, double* crow, float ascale,
-                                          double cscale, bool need_old, int atomic_out) {
+                                          double cscale, bool need_old, int atomic_out,
+                                          uint32_t lead_off = 0) {
   uint32_t r[W];
   if constexpr (W == 32) tmem_ld32(taddr, r);
   else tmem_ld16(taddr, r);
+  if constexpr (SPLIT) {  // small-product sum + leading-product sum, one FP32 rounding
+    uint32_t r2[W];
+    if constexpr (W == 32) tmem_ld32(taddr + lead_off, r2);
+    else tmem_ld16(taddr + lead_off, r2);
+#pragma unroll
+    for (int j = 0; j < W; ++j)
+      r[j] = __float_as_uint(__uint_as_float(r[j]) + __uint_as_float(r2[j]));
+  }
   if (!row_ok) return;
   int cj[W];
   double old[W];
@@ -173,10 +191,10 @@ __device__ __forceinline__ void epi_batch(uint32_t taddr, const int* co, const f
 // chunk's FP32 sum into the FP64 output while the MMA warp fills the other TMEM buffer.
 // Bounding the FP32 accumulation chain keeps the tensor-core accumulator's rounding
 // (truncating, so biased for long sums) at the level of a short dot product.
-template <int BN, int NP>
+template <int BN, int NP, bool SPLIT = false>
 __global__ void __launch_bounds__(GEMM_THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ Maps maps, const Args p) {
-  using L = Smem<BN, NP>;
+  using L = Smem<BN, NP, SPLIT>;
   constexpr int S = L::STAGES;
   constexpr uint32_t TMEM_COLS = L::TMEM_COLS;
   extern __shared__ uint8_t smem_raw[];
@@ -293,8 +311,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
             break;
           }
           tc_fence_after();
-          const uint32_t d = tmem + (uint32_t)(b * BN);
-          uint32_t acc = 0u;
+          const uint32_t d = tmem + (uint32_t)(b * L::ACC);
+          uint32_t acc = 0u, acc_lead = 0u;
           const int npass = (NP == 1) ? p.npass : 1;
           for (int pass = 0; pass < npass && !stop; ++pass) {
             for (int kb = c0; kb < c1; ++kb, ++it) {
@@ -330,8 +348,13 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 for (int pr = 0; pr < 3; ++pr)
 #pragma unroll
                   for (int k = 0; k < 4; ++k) {
-                    umma_f16(d, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc, acc);
-                    acc = 1u;
+                    if (SPLIT && pr == 2) {  // the leading product, own accumulator
+                      umma_f16(d + BN, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc, acc_lead);
+                      acc_lead = 1u;
+                    } else {
+                      umma_f16(d, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc, acc);
+                      acc = 1u;
+                    }
                   }
               }
               umma_commit(&empty[s]);
@@ -396,15 +419,16 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         const double cscale = first ? p.beta : 1.0;  // beta applies once per tile
         const bool need_old = !p.atomic_out && cscale != 0.0;
         double* crow = p.C + roff;
-        const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * BN);
+        const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * L::ACC);
         constexpr int NFULL = BN / 64;  // whole 32-column blocks per warp
 #pragma unroll 1
         for (int fb = 0; fb < NFULL; ++fb)
-          epi_batch<32>(tbase + 32 * (2 * fb + h), colofs + 32 * fb, colsc + 32 * fb, row_ok,
-                        crow, ascale, cscale, need_old, p.atomic_out);
+          epi_batch<32, SPLIT>(tbase + 32 * (2 * fb + h), colofs + 32 * fb, colsc + 32 * fb,
+                               row_ok, crow, ascale, cscale, need_old, p.atomic_out, BN);
         if constexpr (BN % 64 != 0)  // BN = 96, 160, 224: the last block split 16 / 16
-          epi_batch<16>(tbase + (BN - 32) + 16 * h, colofs + 32 * NFULL, colsc + 32 * NFULL,
-                        row_ok, crow, ascale, cscale, need_old, p.atomic_out);
+          epi_batch<16, SPLIT>(tbase + (BN - 32) + 16 * h, colofs + 32 * NFULL,
+                               colsc + 32 * NFULL, row_ok, crow, ascale, cscale, need_old,
+                               p.atomic_out, BN);
         first = false;
         tc_fence_before();
         __syncwarp();
@@ -704,18 +728,19 @@ int num_sms() {
   return sms;
 }
 
-template <int BN, int NP = 1>
+template <int BN, int NP = 1, bool SPLIT = false>
 int launch(const Maps& maps, Args a, cudaStream_t st) {
   static bool attr = false;
-  const int smem = Smem<BN, NP>::TOTAL;
+  const int smem = Smem<BN, NP, SPLIT>::TOTAL;
   if (!attr) {
-    cudaFuncSetAttribute(tc_gemm_kernel<BN, NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(tc_gemm_kernel<BN, NP, SPLIT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
   a.nt = (a.N + BN - 1) / BN;
   const long long ntiles = a.mt * a.nt * a.splits;
   const long long grid = std::min<long long>(ntiles, num_sms());
-  tc_gemm_kernel<BN, NP><<<(unsigned)grid, GEMM_THREADS, smem, st>>>(maps, a);
+  tc_gemm_kernel<BN, NP, SPLIT><<<(unsigned)grid, GEMM_THREADS, smem, st>>>(maps, a);
   PCG_CHECK_LAUNCH("pcg_tc_gemm");
   return 0;
 }
@@ -777,7 +802,7 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   PackArgs p{};
   if (!fill_pack(p.r, r_n, r_ext, r_str) || !fill_pack(p.k, k_n, k_ext, k_str)) return -1;
   p.row_tab = row_tab;
-  if (fmt == kBF16x3F) fmt = kBF16x3;  // same operand pieces; the GEMM differs
+  if (fmt == kBF16x3F || fmt == kBF16x3S) fmt = kBF16x3;  // same pieces; the GEMM differs
   if (fmt < 0 || fmt > 3 || (!X && !P) || !hi || ((fmt == kBF16x3 || fmt == kBF16x6) && !lo) ||
       (fmt == kBF16x6 && !mid) || (fmt == kFP8 && !row_scale) || (P && !Q)) {
     set_error("pcg_pack_operand: bad pointers for format %d", fmt);
@@ -863,13 +888,14 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
                            const long long* n_ext, const long long* n_sc,
                            const long long* col_map, const double* col_scale, double alpha,
                            double beta, double* C, int* status, void* stream) {
-  if (fmt < 0 || fmt > 4) {
+  if (fmt < 0 || fmt > 5) {
     set_error("pcg_tc_gemm: unknown format %d", fmt);
     return -1;
   }
   const int eb = (fmt == kFP8) ? 1 : 2;
   const int kblk = KBYTES / eb;
-  const bool need_lo = (fmt == kBF16x3 || fmt == kBF16x6 || fmt == kBF16x3F);
+  const bool need_lo =
+      (fmt == kBF16x3 || fmt == kBF16x6 || fmt == kBF16x3F || fmt == kBF16x3S);
   if (!A_hi || !B_hi || !C || !status || (need_lo && (!A_lo || !B_lo)) ||
       (fmt == kBF16x6 && (!A_mid || !B_mid)) || (fmt == kFP8 && (!a_scale || !b_scale))) {
     set_error("pcg_tc_gemm: null pointer for format %d", fmt);
@@ -921,11 +947,13 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   // with fewer tiles than SMs is split along K instead) and weighting each tile by its
   // columns plus its fixed A-operand share.
   static const int kBN[] = {64, 96, 128, 160, 192, 224, 256};
-  const bool fused = (fmt == kBF16x3F);
+  const bool fused = (fmt == kBF16x3F || fmt == kBF16x3S);
+  const bool split_acc = (fmt == kBF16x3S);
   const long long sms_all = num_sms();
   int BN = 64;
   long long best = -1;
   for (int bn : kBN) {
+    if (split_acc && bn > 128) continue;  // four accumulators in 512 TMEM columns
     const long long tiles = ((M + BM - 1) / BM) * ((N + bn - 1) / bn);
     const long long slots = tiles >= sms_all ? (tiles + sms_all - 1) / sms_all * sms_all : tiles;
     const long long cost = slots * (bn + 48);
@@ -956,7 +984,8 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.kb_per_split = kps;
   // FP32 accumulation chain per FP64 flush: 4096 K for split-BF16x3 (fused or by passes),
   // 2048 K for BF16x6, 12288 K for single BF16.
-  a.kb_chunk = (fmt == kBF16x3 || fmt == kBF16x3F) ? 64 : (fmt == kBF16x6 ? 32 : 192);
+  a.kb_chunk = (fmt == kBF16x3 || fmt == kBF16x3F || fmt == kBF16x3S) ? 64
+                                                                      : (fmt == kBF16x6 ? 32 : 192);
   a.atomic_out = splits > 1;
   cudaStream_t st = (cudaStream_t)stream;
   if (a.atomic_out && beta != 1.0) {
@@ -970,6 +999,13 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   for (int q = 0; q < 3; ++q) {
     if (!make_map(&maps.a[q], pa[q] ? pa[q] : A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
     if (!make_map(&maps.b[q], pb[q] ? pb[q] : B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
+  }
+  if (split_acc) {
+    switch (BN) {
+      case 64: return launch<64, 2, true>(maps, a, st);
+      case 96: return launch<96, 2, true>(maps, a, st);
+      default: return launch<128, 2, true>(maps, a, st);
+    }
   }
   if (fused) {
     switch (BN) {

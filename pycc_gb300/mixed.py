@@ -22,8 +22,8 @@ import torch
 
 from . import _lib
 from .contract import contract_f64
-from .tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X6, FMT_FP8, Operand, TCEngine, pack,
-                 static_pack_format)
+from .tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_BF16X6, FMT_FP8, Operand,
+                 TCEngine, pack, static_pack_format)
 
 
 class MixedResidual:
@@ -48,8 +48,8 @@ class MixedResidual:
         elif mode == "bf16x3":
             self.stages = ["bf16x3"]
         else:
-            self.stages = (["fp8", "bf16", "bf16x3f", "bf16x3"] if w.vvvv_fp8
-                           else ["bf16", "bf16x3f", "bf16x3"])
+            self.stages = (["fp8", "bf16", "bf16x3f", "bf16x3s"] if w.vvvv_fp8
+                           else ["bf16", "bf16x3f", "bf16x3s"])
         self.stage = 0
         self.thresholds = {"fp8": getattr(w, "fp8_threshold", 1e-3), "bf16": w.switch_threshold,
                            "bf16x3f": 0.0}
@@ -110,8 +110,8 @@ class MixedResidual:
     def mode_name(self):
         return self.stages[self.stage]
 
-    FMTS = {"bf16": FMT_BF16, "bf16x3f": FMT_BF16X3F, "bf16x3": FMT_BF16X3, "bf16x6": FMT_BF16X6,
-            "fp8": FMT_BF16}
+    FMTS = {"bf16": FMT_BF16, "bf16x3f": FMT_BF16X3F, "bf16x3s": FMT_BF16X3S,
+            "bf16x3": FMT_BF16X3, "bf16x6": FMT_BF16X6, "fp8": FMT_BF16}
 
     def fmt(self):
         return self.FMTS[self.mode_name()]

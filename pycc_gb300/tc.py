@@ -20,12 +20,13 @@ import torch
 
 from . import _lib
 
-FMT_BF16, FMT_BF16X3, FMT_FP8, FMT_BF16X6, FMT_BF16X3F = 0, 1, 2, 3, 4
+FMT_BF16, FMT_BF16X3, FMT_FP8, FMT_BF16X6, FMT_BF16X3F, FMT_BF16X3S = 0, 1, 2, 3, 4, 5
 
 
 def pack_format(fmt):
-    """The operand pieces a GEMM format reads (fused and by-pass split-BF16x3 share them)."""
-    return FMT_BF16X3 if fmt == FMT_BF16X3F else fmt
+    """The operand pieces a GEMM format reads (the split-BF16x3 GEMMs, fused, fused with
+    separate accumulators or by passes, share them)."""
+    return FMT_BF16X3 if fmt in (FMT_BF16X3F, FMT_BF16X3S) else fmt
 
 
 def static_pack_format(fmt):

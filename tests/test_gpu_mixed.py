@@ -10,18 +10,19 @@ import pytest
 import torch
 
 import pycc_gb300 as pg
-from pycc_gb300.tc import FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_FP8, Operand, TCEngine
+from pycc_gb300.tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_FP8, Operand,
+                           TCEngine)
 from oracle import ccsd as oc
 
 pytestmark = pytest.mark.gpu
-TOL = {FMT_BF16: 2e-2, FMT_BF16X3: 5e-5, FMT_BF16X3F: 5e-5, FMT_FP8: 8e-2}
+TOL = {FMT_BF16: 2e-2, FMT_BF16X3: 5e-5, FMT_BF16X3F: 5e-5, FMT_BF16X3S: 5e-5, FMT_FP8: 8e-2}
 
 
 def frob(a, b):
     return (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
 
 
-@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_FP8])
+@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_FP8])
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (200, 70, 100), (37, 300, 513), (64, 180, 96),
                                    (100, 210, 64), (150, 150, 64), (300, 820, 200)])
 def test_gemm_exact_integers(cuda, fmt, M, N, K):
@@ -41,7 +42,7 @@ def test_gemm_exact_integers(cuda, fmt, M, N, K):
     assert torch.equal(out, ref)
 
 
-@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_FP8])
+@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_FP8])
 def test_gemm_random_error(cuda, fmt):
     g = torch.Generator(device=cuda).manual_seed(5)
     A = torch.randn(333, 1000, generator=g, device=cuda, dtype=torch.float64)

@@ -7,8 +7,8 @@ import pytest
 import torch
 
 import pycc_gb300.tc as tc
-from pycc_gb300.tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X6, FMT_FP8, Operand,
-                           Packed, TCEngine, static_pack_format)
+from pycc_gb300.tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_BF16X6, FMT_FP8,
+                           Operand, Packed, TCEngine, static_pack_format)
 
 
 @pytest.fixture
@@ -93,6 +93,7 @@ def test_static_and_dynamic_caches(recorder):
 def test_static_pack_formats():
     assert static_pack_format(FMT_BF16) == FMT_BF16X3
     assert static_pack_format(FMT_BF16X3F) == FMT_BF16X3
+    assert static_pack_format(FMT_BF16X3S) == FMT_BF16X3
     assert static_pack_format(FMT_BF16X3) == FMT_BF16X3
     assert static_pack_format(FMT_FP8) == FMT_FP8
     assert static_pack_format(FMT_BF16X6) == FMT_BF16X6
@@ -107,7 +108,7 @@ def test_ladder_prunes_formats_no_later_stage_reads():
         device1, stream, vvvv_fp8, switch_threshold = "cpu", None, True, 1e-5
 
     m = MixedResidual(W())
-    assert m.stages == ["fp8", "bf16", "bf16x3f", "bf16x3"]
+    assert m.stages == ["fp8", "bf16", "bf16x3f", "bf16x3s"]
     m.tc.cache = {("ERI", "vvvv", FMT_FP8): 1, ("ERI", "ovvv", FMT_BF16X3): 2}
     m._advance()                                         # fp8 -> bf16
     assert list(m.tc.cache) == [("ERI", "ovvv", FMT_BF16X3)]
