@@ -241,6 +241,10 @@ bool fill_sub(SubIdx& d, int n, const long long* ext, const long long* s0, const
     set_error("pcg_contract_f64: %s has %d sub-indices (max %d)", what, n, kMaxSub);
     return false;
   }
+  if (n > 0 && (!ext || !s0 || !s1)) {
+    set_error("pcg_contract_f64: %s extents or strides missing", what);
+    return false;
+  }
   d.n = n;
   for (int q = 0; q < n; ++q) {
     if (ext[q] <= 0) {
@@ -516,8 +520,9 @@ extern "C" int pcg_contract_multi_f64(int nterm, int m_n, const long long* m_ext
                                       double beta, double* C, void* stream) {
   using namespace pcg;
   if (nterm < 1 || nterm > kMaxTerms || m_n < 0 || m_n > kMaxSub || n_n < 0 || n_n > kMaxSub ||
-      !C) {
-    set_error("pcg_contract_multi_f64: bad term / sub-index counts");
+      !C || !k_n || !alpha || !A || !B || (m_n > 0 && !m_sa) || (n_n > 0 && !n_sb) ||
+      !k_ext || !k_sa || !k_sb) {
+    set_error("pcg_contract_multi_f64: bad term / sub-index counts or missing arrays");
     return -1;
   }
   MultiArgs p{};

@@ -411,7 +411,7 @@ extern "C" int pcg_combine4_f64(const long long* ext, double a, const double* X,
                                 const long long* xs, double b, const double* Y,
                                 const long long* ys, double* out, const long long* os,
                                 void* stream) {
-  if (!X || !out) {
+  if (!X || !out || !ext || !xs || !os || (Y && !ys)) {
     set_error("pcg_combine4_f64: null pointer");
     return -1;
   }
@@ -457,6 +457,10 @@ extern "C" int pcg_symmetrize_f64(const double* h, long long no, long long nv, d
 extern "C" int pcg_update_amps_f64(double* t1, double* t2, const double* r1, const double* r2,
                                    const double* eps, long long no, long long nv, double* work,
                                    long long work_len, double* rms2, void* stream) {
+  if (!t1 || !t2 || !r1 || !r2 || !eps || !work || !rms2) {
+    set_error("pcg_update_amps_f64: null pointer");
+    return -1;
+  }
   if (!check_work(work_len, RED_BLOCKS, "pcg_update_amps_f64")) return -1;
   if (no <= 0 || nv <= 0 || no * no * nv * nv > 0x7fffffffLL) {
     set_error("pcg_update_amps_f64: o^2 v^2 must be in [1, 2^31)");
@@ -476,6 +480,10 @@ extern "C" int pcg_energy_f64(const double* fov, const long long* fs, const doub
                               const long long* ls, const double* t1, const double* t2,
                               long long no, long long nv, double* work, long long work_len,
                               double* out, void* stream) {
+  if (!fov || !fs || !L || !ls || !t1 || !t2 || !work || !out) {
+    set_error("pcg_energy_f64: null pointer");
+    return -1;
+  }
   if (!check_work(work_len, RED_BLOCKS, "pcg_energy_f64")) return -1;
   cudaStream_t st = (cudaStream_t)stream;
   Strides4 s{};
@@ -499,6 +507,15 @@ extern "C" int pcg_dots_f64(const double* x, const double* const* ys, int k, lon
     set_error("pcg_dots_f64: k=%d outside [1, %d]", k, kMaxVec);
     return -1;
   }
+  if (!x || !ys || !work || !out || n < 0) {
+    set_error("pcg_dots_f64: null pointer or negative length");
+    return -1;
+  }
+  for (int j = 0; j < k; ++j)
+    if (!ys[j]) {
+      set_error("pcg_dots_f64: vector %d is null", j);
+      return -1;
+    }
   if (!check_work(work_len, (long long)k * RED_BLOCKS, "pcg_dots_f64")) return -1;
   cudaStream_t st = (cudaStream_t)stream;
   VecList v{};
@@ -517,6 +534,15 @@ extern "C" int pcg_lincomb_f64(const double* const* xs, const double* c, int k, 
     set_error("pcg_lincomb_f64: k=%d outside [1, %d]", k, kMaxVec);
     return -1;
   }
+  if (!xs || !c || !out || n < 0) {
+    set_error("pcg_lincomb_f64: null pointer or negative length");
+    return -1;
+  }
+  for (int j = 0; j < k; ++j)
+    if (!xs[j]) {
+      set_error("pcg_lincomb_f64: input %d is null", j);
+      return -1;
+    }
   VecList v{};
   for (int j = 0; j < k; ++j) {
     v.p[j] = xs[j];
@@ -567,10 +593,15 @@ extern "C" int pcg_diis_error_f64(const double* x, const double* old, double* e,
     set_error("pcg_diis_error_f64: k=%d outside [1, %d]", k, kMaxVec);
     return -1;
   }
-  if (!x || !old || !e || e == x || e == old) {
+  if (!x || !old || !e || e == x || e == old || !work || !out || n < 0 || (k > 1 && !ys)) {
     set_error("pcg_diis_error_f64: bad pointers");
     return -1;
   }
+  for (int j = 0; j + 1 < k; ++j)
+    if (!ys[j]) {
+      set_error("pcg_diis_error_f64: stored error vector %d is null", j);
+      return -1;
+    }
   if (!check_work(work_len, (long long)k * RED_BLOCKS, "pcg_diis_error_f64")) return -1;
   cudaStream_t st = (cudaStream_t)stream;
   VecList v{};
@@ -592,7 +623,7 @@ extern "C" int pcg_diis_error_f32(const double* x, const double* old, float* e,
     set_error("pcg_diis_error_f32: k=%d outside [1, %d]", k, kMaxVec);
     return -1;
   }
-  if (!x || !old || !e || !out || n < 0) {
+  if (!x || !old || !e || !out || !work || n < 0 || (k > 1 && !ys)) {
     set_error("pcg_diis_error_f32: bad arguments");
     return -1;
   }
@@ -727,7 +758,7 @@ extern "C" int pcg_inv_denominators_f64(const double* eps, long long no, long lo
 // *rms2 = sum (r*inv)^2.  work >= 1024 doubles.  solve_cc update (pycc/ccwfn.py:281-284).
 extern "C" int pcg_update_inv_f64(double* t, const double* r, const double* inv, long long n,
                                   double* work, long long work_len, double* rms2, void* stream) {
-  if (!t || !r || !inv || !rms2 || n < 0) {
+  if (!t || !r || !inv || !rms2 || !work || n < 0) {
     set_error("pcg_update_inv_f64: bad arguments");
     return -1;
   }

@@ -750,6 +750,10 @@ bool fill_epi(EpiIdx& d, int n, const long long* ext, const long long* s, const 
     set_error("pcg_tc_gemm: %s has %d sub-indices (max %d)", what, n, kMaxSub);
     return false;
   }
+  if (n > 0 && (!ext || !s)) {
+    set_error("pcg_tc_gemm: %s extents or strides missing", what);
+    return false;
+  }
   d.n = n ? n : 1;
   if (!n) {
     d.ext[0] = 1;
@@ -769,6 +773,10 @@ bool fill_epi(EpiIdx& d, int n, const long long* ext, const long long* s, const 
 bool fill_pack(PackIdx& d, int n, const long long* ext, const long long* str) {
   if (n < 0 || n > kMaxSub) {
     set_error("pcg_pack_operand: %d sub-indices (max %d)", n, kMaxSub);
+    return false;
+  }
+  if (n > 0 && (!ext || !str)) {
+    set_error("pcg_pack_operand: extents or strides missing");
     return false;
   }
   d.n = n ? n : 1;

@@ -272,7 +272,8 @@ extern "C" int pcg_tc_grouped_gemm(int na, const void* const* a_ptr, const long 
                                    float* C, long long ldm, long long ldn, int* status,
                                    void* stream) {
   if (na < 1 || na > 4 || nb < 1 || nb > 4 || !groups || ngroups < 1 || M < 1 || N < 1 || !C ||
-      !status || ldm < 1 || ldn < 1 || M > 0x7fffffffLL || N > 0x7fffffffLL) {
+      !status || ldm < 1 || ldn < 1 || M > 0x7fffffffLL || N > 0x7fffffffLL || !a_ptr ||
+      !a_rows || !a_ld || !b_ptr || !b_rows || !b_ld) {
     set_error("pcg_tc_grouped_gemm: bad arguments");
     return -1;
   }
