@@ -170,7 +170,9 @@ __host__ __device__ constexpr int kord(int so, int q) {
   return (int)((0x192261624ULL >> (2 * (3 * so + q))) & 3u);
 }
 
-__global__ void __launch_bounds__(TE2_THREADS) triples_energy_tiled_kernel(
+// five resident blocks per SM (48 registers): short, latency-bound blocks gain more from the
+// extra block than they lose to the few spilled registers of the staging phase
+__global__ void __launch_bounds__(TE2_THREADS, 5) triples_energy_tiled_kernel(
     const TripArgs<float> p, long long ntt) {
   __shared__ TiledStage s;
   const int t = blockIdx.y;
