@@ -576,8 +576,10 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
 
 // BF16 / split-BF16x3 from an FP32 tile: two adjacent K entries per thread, written as one
 // bf16x2 word (K offsets are even: Kp and k0 are multiples of 64).
+// eight resident blocks per SM (32 registers): the pack waits on memory latency, and the
+// extra blocks hide more of it than the few spilled registers cost
 template <bool KF>
-__global__ void __launch_bounds__(PACK_THREADS) pack_bf16_kernel(const PackArgs p) {
+__global__ void __launch_bounds__(PACK_THREADS, 8) pack_bf16_kernel(const PackArgs p) {
   __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
   pack_tile_load<float, KF>(p, t, r0, k0);
