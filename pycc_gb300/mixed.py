@@ -292,16 +292,21 @@ class MixedResidual:
     def residuals(self, F, t1, t2):
         t1 = t1.contiguous()
         t2 = t2.contiguous()
-        self.tc.dyn_cache = {}          # identical dynamic operands are packed once per call
-        Fae = self.build_Fae(F, t1, t2)
-        Fmi = self.build_Fmi(F, t1, t2)
-        Fme = self.build_Fme(F, t1)
-        Wmnij = self.build_Wmnij(t1, t2)
-        Wmbej = self.build_Wmbej(t1, t2)
-        Wmbje = self.build_Wmbje(t1, t2)
-        Zmbij = self.build_Zmbij(t1, t2)
-        r1 = self.r_T1(F, t1, t2, Fae, Fme, Fmi)
-        half = self.r_T2_half(F, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij)
+        # identical dynamic operands are packed once per call; the packs are released
+        # when the call returns
+        self.tc.dyn_cache = {}
+        try:
+            Fae = self.build_Fae(F, t1, t2)
+            Fmi = self.build_Fmi(F, t1, t2)
+            Fme = self.build_Fme(F, t1)
+            Wmnij = self.build_Wmnij(t1, t2)
+            Wmbej = self.build_Wmbej(t1, t2)
+            Wmbje = self.build_Wmbje(t1, t2)
+            Zmbij = self.build_Zmbij(t1, t2)
+            r1 = self.r_T1(F, t1, t2, Fae, Fme, Fmi)
+            half = self.r_T2_half(F, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij)
+        finally:
+            self.tc.dyn_cache = None
         r2 = torch.empty_like(half)
         _lib.call("pcg_symmetrize_f64", half.data_ptr(), self.w.no, self.w.nv, r2.data_ptr(),
                   _lib.stream_handle(self.w.stream))

@@ -36,6 +36,8 @@ def static_pack_format(fmt):
     packing every integral block again."""
     f = pack_format(fmt)
     return FMT_BF16X3 if f == FMT_BF16 else f
+
+
 MAX_SUB = 4
 
 
@@ -263,11 +265,14 @@ class TCEngine:
             src = tuple((s[0].data_ptr(), tuple(s[0].stride()), s[1]) if s is not None else None
                         for s in op.sources())
             dkey = (src, op.a, op.b, op.c, op.labels, tuple(rows), tuple(ks), pack_format(fmt))
-            p = self.dyn_cache.get(dkey)
-            if p is None:
-                p = pack(op, rows, ks, fmt, self.stream)
-                self.dyn_cache[dkey] = p
-            return p
+            hit = self.dyn_cache.get(dkey)
+            if hit is None:
+                # the entry holds its source tensors, so no later tensor can reuse their
+                # addresses while the cache lives
+                hit = (pack(op, rows, ks, fmt, self.stream),
+                       [s[0] for s in op.sources() if s is not None])
+                self.dyn_cache[dkey] = hit
+            return hit[0]
         # the operand's own label string fixes which tensor axis each label names
         sf = static_pack_format(fmt)
         key = (op.key, op.labels, tuple(rows), tuple(ks), sf)

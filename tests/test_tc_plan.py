@@ -88,6 +88,9 @@ def test_static_and_dynamic_caches(recorder):
     for _ in range(3):
         eng.contract("jf,mbef->mbej", Operand.of("jf", t1), V, t(o, v, v, o), fmt=FMT_BF16X3)
     assert len(recorder["pack"]) == n0 + 1                # t1 packed once per residual
+    # the entry keeps its source alive, so its address cannot be reused for another tensor
+    (entry,) = eng.dyn_cache.values()
+    assert any(s is t1 for s in entry[1])
 
 
 def test_static_pack_formats():
