@@ -85,3 +85,24 @@ def test_residuals_o20v180_golden():
     assert rel(r2[0, 1], g["r2_slice_ij01"]) < 1e-12
     assert rel(r2[:, :, 0, 0], g["r2_slice_ab00"]) < 1e-12
     assert np.linalg.norm(r2) == pytest.approx(float(g["r2_norm"]), rel=1e-12)
+
+
+def test_triples_oracle_golden_o5v19(golden_o5v19, ham_o5v19):
+    """The (T) oracle (Lee-Rendell over i >= j >= k, and the full-(i, j, k) X1/X2 form) on the
+    reference's converged amplitudes against the reference's own t_tjl and t_vikings."""
+    from oracle import triples as ot
+    _, F, ERI, L = ham_o5v19
+    t1, t2 = golden_o5v19["t1"], golden_o5v19["t2"]
+    assert ot.t_tjl(5, 19, F, ERI, t1, t2) == pytest.approx(float(golden_o5v19["et_tjl"]), abs=1e-14)
+    assert ot.t_vikings(5, 19, F, ERI, L, t1, t2) == pytest.approx(float(golden_o5v19["et_vikings"]),
+                                                                    abs=1e-14)
+
+
+def test_density_fixture_energy_identity(golden_o5v19, ham_o5v19):
+    """The reference's gradient densities reproduce its correlation energy,
+    E = <D, F> + <Gamma, ERI> (the identity of pycc/tests/test_076_ccsd_gradient.py:103-111):
+    the D and Gamma fixtures the GPU adjoint is compared with are consistent."""
+    _, F, ERI, _ = ham_o5v19
+    E = float(np.sum(golden_o5v19["D"] * F) + np.sum(golden_o5v19["Gamma"] * ERI))
+    assert E == pytest.approx(float(golden_o5v19["ecc"]), abs=1e-12)
+    assert E == pytest.approx(float(golden_o5v19["E_from_densities"]), abs=1e-12)
