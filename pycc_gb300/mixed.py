@@ -59,6 +59,27 @@ class MixedResidual:
         self.profile = None       # list of (subscripts, fmt, start, end) events when set
         self._pairs = None        # i <= j pair tables of the ladder
         self._r_seed = None
+        self._blocks = None       # the integral blocks the caches were built from
+
+    def sync_integrals(self):
+        """Drop the packed integrals and the 1/2 <ab|ij> seed when ``H.ERI`` / ``H.L`` no
+        longer hold the blocks they were built from.  The reference's derivative driver swaps
+        them for derivative integrals around one ``residuals`` call, using the residual's
+        linearity in H (pycc/ccderiv.py:252-259); the next call after each swap re-packs.
+        The blocks are referenced here, so their addresses cannot be reused unnoticed."""
+        H = self.w.H
+        try:
+            blocks = list(H.ERI.blocks.values()) + list(H.L.blocks.values())
+        except AttributeError:
+            raise TypeError("H.ERI and H.L must be pycc_gb300 BlockTensors (resident o/v "
+                            "blocks), e.g. Hamiltonian.from_arrays(...).ERI") from None
+        if self._blocks is not None and len(blocks) == len(self._blocks) and all(
+                a is b for a, b in zip(blocks, self._blocks)):
+            return
+        if self._blocks is not None:
+            self.tc.cache.clear()
+            self._r_seed = None
+        self._blocks = blocks
 
     # -- precision schedule ---------------------------------------------------------------
     def select_mode(self, rms):
@@ -292,6 +313,7 @@ class MixedResidual:
     def residuals(self, F, t1, t2):
         t1 = t1.contiguous()
         t2 = t2.contiguous()
+        self.sync_integrals()
         # identical dynamic operands are packed once per call; the packs are released
         # when the call returns
         self.tc.dyn_cache = {}

@@ -118,3 +118,43 @@ def test_ladder_prunes_formats_no_later_stage_reads():
     m._advance()
     m._advance()                                         # split stages keep the pack
     assert list(m.tc.cache) == [("ERI", "ovvv", FMT_BF16X3)]
+
+
+def test_swapped_integrals_drop_the_packs():
+    """A caller that swaps H.ERI / H.L for other blocks (the reference's linear-in-H use of
+    the residual, pycc/ccderiv.py:252-259) gets its integrals re-packed, not the cached
+    packs of the previous blocks."""
+    from pycc_gb300.hamiltonian import BlockTensor
+    from pycc_gb300.mixed import MixedResidual
+
+    def blocks(name):
+        return BlockTensor(name, 2, 3, {"oovv": t(2, 2, 3, 3), "ovvv": t(2, 3, 3, 3)})
+
+    class Ham:
+        def __init__(self):
+            self.ERI, self.L = blocks("ERI"), blocks("L")
+
+    class W:
+        device1, stream, vvvv_fp8, switch_threshold = "cpu", None, True, 1e-5
+
+        def __init__(self):
+            self.h = self.H = Ham()
+
+    w = W()
+    m = MixedResidual(w)
+    m.sync_integrals()
+    m.tc.cache = {("ERI", "ovvv", FMT_BF16X3): 1}
+    m._r_seed = "seed"
+    m.sync_integrals()                                  # same blocks: caches kept
+    assert m.tc.cache and m._r_seed == "seed"
+    saved = w.h.ERI
+    w.h.ERI = blocks("ERI")                             # derivative integrals swapped in
+    m.sync_integrals()
+    assert not m.tc.cache and m._r_seed is None
+    m.tc.cache = {("ERI", "ovvv", FMT_BF16X3): 2}
+    w.h.ERI = saved                                     # and swapped back
+    m.sync_integrals()
+    assert not m.tc.cache
+    w.h.ERI = t(5, 5, 5, 5)                             # a plain array is refused
+    with pytest.raises(TypeError):
+        m.sync_integrals()
