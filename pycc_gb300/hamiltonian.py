@@ -60,6 +60,13 @@ def _sl(pat, no, nv):
     return [slice(0, no) if c == "o" else slice(no, no + nv) for c in pat]
 
 
+def _host(x):
+    """A float64 numpy view or copy of a numpy array or torch tensor (any device)."""
+    if isinstance(x, torch.Tensor):
+        x = x.detach().to("cpu", torch.float64).numpy()
+    return np.asarray(x, dtype=np.float64)
+
+
 class Hamiltonian:
     """``H.F``, ``H.eps``, ``H.ERI``, ``H.L`` of the reference, resident on one GPU."""
 
@@ -74,9 +81,12 @@ class Hamiltonian:
 
     @classmethod
     def from_arrays(cls, F, ERI, no, L=None, device="cuda:0"):
-        """Upload the needed blocks of host (numpy) arrays in the reference's layout."""
+        """Upload the needed blocks of full nmo x nmo / nmo^4 arrays in the reference's layout
+        (numpy arrays, or torch tensors on any device, as the reference's CPU and GPU modes
+        hold them)."""
         device = torch.device(device)
-        F = np.asarray(F, dtype=np.float64)
+        F, ERI = _host(F), _host(ERI)
+        L = None if L is None else _host(L)
         n = F.shape[0]
         nv = n - no
         eri = {}
