@@ -202,6 +202,96 @@ class CCSDAdjoint:
         accumulate(gh, gO, stream=self.stream)
         accumulate(gh, gO, perm=(1, 0, 3, 2), stream=self.stream)
 
+    # -- forward (tangent) sweep: the Jacobian action -------------------------------------
+    def forward_tangent(self, x1, x2):
+        """Tangents of every taped tensor along the amplitude direction (x1, x2), by one pass
+        over the tape in recording order.  Each taped operation is linear or bilinear in its
+        inputs, so the tangents are exact derivatives, not difference quotients.  Tensors
+        with no tangent buffer (the integrals and everything built from them alone) are
+        constant along (x1, x2)."""
+        no, nv = self.w.no, self.w.nv
+        for x, shape in ((x1, (no, nv)), (x2, (no, no, nv, nv))):
+            if (not isinstance(x, torch.Tensor) or tuple(x.shape) != shape
+                    or x.dtype != torch.float64 or x.device != self.t2.device):
+                raise ValueError("jacobian: X1, X2 must be float64 tensors of shapes %s, %s on %s"
+                                 % ((no, nv), (no, no, nv, nv), self.t2.device))
+        T = Grads()
+        accumulate(T.get(self.t1), x1, stream=self.stream)
+        accumulate(T.get(self.t2), x2, stream=self.stream)
+        for kind, args in self.tape.ops:
+            getattr(self, "_fw_" + kind)(T, *args)
+        return T
+
+    def _fw_contract(self, T, subs, A, B, out, alpha, beta):
+        ta = T.get(A) if T.has(A) else None
+        tb = T.get(B) if T.has(B) else None
+        if ta is None and tb is None:
+            return
+        to = T.get(out)
+        b = beta                      # 0 for a fresh output: the first term writes it
+        if ta is not None:
+            contract_f64(subs, ta, B, out=to, alpha=alpha, beta=b, stream=self.stream)
+            b = 1.0
+        if tb is not None:
+            contract_f64(subs, A, tb, out=to, alpha=alpha, beta=b, stream=self.stream)
+
+    def _fw_copy(self, T, X, out):
+        if T.has(X):
+            accumulate(T.get(out), T.get(X), stream=self.stream)
+
+    def _fw_combine(self, T, a, X, b, Y, perm, out):
+        use_x = a != 0.0 and T.has(X)
+        use_y = Y is not None and b != 0.0 and T.has(Y)
+        if not (use_x or use_y):
+            return
+        to = T.get(out)
+        if use_x:
+            accumulate(to, T.get(X), a, stream=self.stream)
+        if use_y:
+            accumulate(to, T.get(Y), b, perm=perm, stream=self.stream)
+
+    def _fw_tau(self, T, t1, t2, f1, f2, out):
+        use2 = f1 != 0.0 and T.has(t2)
+        use1 = f2 != 0.0 and T.has(t1)
+        if not (use1 or use2):
+            return
+        to = T.get(out)
+        if use2:
+            accumulate(to, T.get(t2), f1, stream=self.stream)
+        if use1:
+            d1 = T.get(t1)
+            contract_f64("ia,jb->ijab", d1, t1, out=to, alpha=f2, beta=1.0, stream=self.stream)
+            contract_f64("ia,jb->ijab", t1, d1, out=to, alpha=f2, beta=1.0, stream=self.stream)
+
+    def _fw_sym(self, T, h, out):
+        if T.has(h):
+            to, th = T.get(out), T.get(h)
+            accumulate(to, th, stream=self.stream)
+            accumulate(to, th, perm=(1, 0, 3, 2), stream=self.stream)
+
+    def jvp(self, x1, x2):
+        """(dr1, dr2, dE): the derivatives of the residual (r2 symmetrised) and of the energy
+        along (x1, x2) at the taped amplitudes."""
+        T = self.forward_tangent(x1, x2)
+        return T.get(self.r1).clone(), T.get(self.r2).clone(), T.get(self.E).clone()
+
+    def jacobian(self, X1, X2):
+        """The CCSD Jacobian applied to an amplitude pair, ``CCderiv._ccsd_jacobian(X1, X2,
+        hbar)`` (pycc/ccderiv.py:149-180), without HBAR: the tangent of the residual itself.
+
+        Returns (sigma1, sigma2) in the reference's convention: sigma2 is the doubles part
+        before symmetrisation, so sigma2 + sigma2.swapaxes(0,1).swapaxes(2,3) is the doubles
+        action, as the reference's callers form it (pycc/ccderiv.py:267-270).  Only that sum
+        is defined by the residual; sigma2 is returned as half of it."""
+        T = self.forward_tangent(X1, X2)
+        s1 = T.get(self.r1).clone()
+        d2 = T.get(self.r2)
+        s2 = torch.empty_like(d2)
+        _lib.call("pcg_combine4_f64", _lib.i64s(d2.shape), 0.5, d2.data_ptr(),
+                  _lib.i64s(d2.stride()), 0.0, None, _lib.i64s([0, 0, 0, 0]), s2.data_ptr(),
+                  _lib.i64s(s2.stride()), _lib.stream_handle(self.stream))
+        return s1, s2
+
     # -- Lambda equations -----------------------------------------------------------------
     def dE_dt(self):
         G = self.backward(gE=1.0)

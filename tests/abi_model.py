@@ -1,0 +1,152 @@
+"""numpy model of the FP64 C-ABI entry points, for CPU tests of the host logic only.
+
+Each function restates the documented semantics of one entry point of
+``include/pycc_gb300.h`` on tensors in host memory (``data_ptr()`` of a CPU tensor is a host
+address).  Tests install it in place of ``pycc_gb300._lib.call`` to run the host code of the
+FP64 engine -- the builders' contraction plans, the adjoint tape and its sweeps, the solver
+loops, DIIS -- without a GPU.  The CUDA kernels themselves are checked against the oracle in
+the ``-m gpu`` tests; nothing here says anything about them, and nothing outside ``tests/``
+imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+
+def _ints(arr, n):
+    return [int(arr[i]) for i in range(n)]
+
+
+def view(ptr, shape, strides, dtype=np.float64):
+    """A strided numpy view of host memory at ``ptr`` (strides in elements, non-negative)."""
+    if not ptr:
+        raise AssertionError("null pointer")
+    dt = np.dtype(dtype)
+    span = 1 + sum((e - 1) * s for e, s in zip(shape, strides)) if all(e > 0 for e in shape) else 0
+    base = np.frombuffer((C.c_char * (max(span, 1) * dt.itemsize)).from_address(ptr), dtype=dt)
+    return np.lib.stride_tricks.as_strided(base, shape=tuple(shape),
+                                           strides=tuple(s * dt.itemsize for s in strides))
+
+
+def flat(ptr, n, dtype=np.float64):
+    return view(ptr, (n,), (1,), dtype)
+
+
+class ABIModel:
+    """Callable with the signature of ``_lib.call(name, *args)``."""
+
+    def __init__(self):
+        self.calls = []
+
+    def __call__(self, name, *a):
+        self.calls.append(name)
+        fn = getattr(self, name[4:], None)        # strip "pcg_"
+        if fn is None:
+            raise AssertionError("no model of %s" % name)
+        fn(*a)
+        return 0
+
+    # C[m,n] = beta C + alpha sum_k A[m,k] B[n,k]
+    def contract_f64(self, m_n, m_ext, m_sa, m_sc, n_n, n_ext, n_sb, n_sc, k_n, k_ext, k_sa,
+                     k_sb, alpha, A, B, beta, Cp, _st):
+        me, ne, ke = _ints(m_ext, m_n), _ints(n_ext, n_n), _ints(k_ext, k_n)
+        Av = view(A, me + ke, _ints(m_sa, m_n) + _ints(k_sa, k_n))
+        Bv = view(B, ne + ke, _ints(n_sb, n_n) + _ints(k_sb, k_n))
+        Cv = view(Cp, me + ne, _ints(m_sc, m_n) + _ints(n_sc, n_n))
+        prod = np.tensordot(Av, Bv, axes=(list(range(m_n, m_n + k_n)),
+                                          list(range(n_n, n_n + k_n))))
+        res = alpha * prod if beta == 0.0 else beta * Cv + alpha * prod
+        Cv[...] = res
+
+    def combine4_f64(self, ext4, a, X, xs4, b, Y, ys4, out, os4, _st):
+        ext = _ints(ext4, 4)
+        res = a * view(X, ext, _ints(xs4, 4))
+        if Y:
+            res = res + b * view(Y, ext, _ints(ys4, 4))
+        view(out, ext, _ints(os4, 4))[...] = res
+
+    def tau_f64(self, t1, t2, no, nv, f1, f2, out, _st):
+        T1 = view(t1, (no, nv), (nv, 1))
+        T2 = flat(t2, no * no * nv * nv).reshape(no, no, nv, nv)
+        res = f1 * T2 + f2 * np.einsum("ia,jb->ijab", T1, T1)
+        flat(out, no * no * nv * nv).reshape(no, no, nv, nv)[...] = res
+
+    def symmetrize_f64(self, h, no, nv, out, _st):
+        Hh = flat(h, no * no * nv * nv).reshape(no, no, nv, nv)
+        flat(out, no * no * nv * nv).reshape(no, no, nv, nv)[...] = Hh + Hh.transpose(1, 0, 3, 2)
+
+    def energy_f64(self, fov, fs2, L, ls4, t1, t2, no, nv, _work, _wl, out, _st):
+        f = view(fov, (no, nv), _ints(fs2, 2))
+        Lv = view(L, (no, no, nv, nv), _ints(ls4, 4))
+        T1 = view(t1, (no, nv), (nv, 1))
+        T2 = flat(t2, no * no * nv * nv).reshape(no, no, nv, nv)
+        tau = T2 + np.einsum("ia,jb->ijab", T1, T1)
+        flat(out, 1)[0] = 2.0 * np.sum(f * T1) + np.sum(tau * Lv)
+
+    def inv_denominators_f64(self, eps, no, nv, inv1, inv2, _st):
+        e = flat(eps, no + nv)
+        eo, ev = e[:no], e[no:]
+        flat(inv1, no * nv)[...] = (1.0 / (eo[:, None] - ev[None, :])).ravel()
+        d2 = eo[:, None, None, None] + eo[None, :, None, None] - ev[None, None, :, None] - ev
+        flat(inv2, no * no * nv * nv)[...] = (1.0 / d2).ravel()
+
+    def update_inv_f64(self, t, r, inv, n, _work, _wl, out, _st):
+        step = flat(r, n) * flat(inv, n)
+        flat(t, n)[...] += step
+        flat(out, 1)[0] = np.dot(step, step)
+
+    def update_amps_f64(self, t1, t2, r1, r2, eps, no, nv, _work, _wl, out, _st):
+        e = flat(eps, no + nv)
+        eo, ev = e[:no], e[no:]
+        d1 = (eo[:, None] - ev[None, :]).ravel()
+        d2 = (eo[:, None, None, None] + eo[None, :, None, None] - ev[None, None, :, None]
+              - ev).ravel()
+        s1 = flat(r1, no * nv) / d1
+        s2 = flat(r2, no * no * nv * nv) / d2
+        flat(t1, no * nv)[...] += s1
+        flat(t2, no * no * nv * nv)[...] += s2
+        flat(out, 1)[0] = np.dot(s1, s1) + np.dot(s2, s2)
+
+    def _diis_error(self, dt, x, old, e, ys, k, n, out):
+        E = flat(e, n, dt)
+        E[...] = (flat(x, n) - flat(old, n)).astype(dt)
+        e64 = E.astype(np.float64)
+        o = flat(out, k)
+        for j in range(k - 1):
+            o[j] = np.dot(e64, flat(ys[j], n, dt).astype(np.float64))
+        o[k - 1] = np.dot(e64, e64)
+
+    def diis_error_f64(self, x, old, e, ys, k, n, _work, _wl, out, _st):
+        assert 1 <= k <= 16
+        self._diis_error(np.float64, x, old, e, ys, k, n, out)
+
+    def diis_error_f32(self, x, old, e, ys, k, n, _work, _wl, out, _st):
+        assert 1 <= k <= 16
+        self._diis_error(np.float32, x, old, e, ys, k, n, out)
+
+    def lincomb_f64(self, xs, c, k, n, out, _st):
+        assert 1 <= k <= 16 and all(xs[j] != out for j in range(k))
+        acc = np.zeros(n)
+        for j in range(k):
+            acc = acc + c[j] * flat(xs[j], n)
+        flat(out, n)[...] = acc
+
+    lincomb_f64_df = lincomb_f64
+
+
+def install(monkeypatch):
+    """Route the engine's library calls to the model (CPU tensors accepted)."""
+    from pycc_gb300 import _lib, contract
+    model = ABIModel()
+    monkeypatch.setattr(_lib, "call", model)
+    monkeypatch.setattr(_lib, "load", lambda *a, **k: None)
+    monkeypatch.setattr(_lib, "stream_handle", lambda stream=None: None)
+
+    def check(t, name):
+        import torch
+        if not isinstance(t, torch.Tensor) or t.dtype != torch.float64:
+            raise TypeError("contract: %s must be a float64 tensor" % name)
+    monkeypatch.setattr(contract, "_check", check)
+    return model

@@ -8,11 +8,11 @@ with ``CCwfn.__new__`` plus the attributes that ``CCwfn.__init__`` would have se
 (``pycc/ccwfn.py:76-213``, ``pycc/wavefunction.py:293-332``), on the synthetic
 Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
 ``residuals`` / ``solve_cc`` / ``t_vikings`` / ``t_tjl`` / ``cchbar`` -> ``cclambda``
--> ``ccdensity`` and stores their outputs as ``.npz`` fixtures next to this file.
+-> ``ccdensity`` / ``CCderiv._ccsd_jacobian`` and stores their outputs as ``.npz`` fixtures next to this file.
 
 Usage::
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian]
 
 Config 2 (no=20, nv=180) needs ~30 GB of host RAM and several minutes.
 """
@@ -179,6 +179,33 @@ def gen_o5v19(pycc):
              len(energies) - 1))
 
 
+def gen_o5v19_jacobian(pycc):
+    """The reference's CCSD Jacobian action at the converged no=5, nv=19 amplitudes:
+    ``CCderiv._ccsd_jacobian(X1, X2, hbar)`` (pycc/ccderiv.py:149-180) on a seeded amplitude
+    pair X (X2_ijab = X2_jiba), called with the two attributes it reads (``contract`` and
+    ``ccwfn``) instead of a full CCderiv, whose set-up needs psi4."""
+    no, nv, seed = WORKLOADS["o5v19"]
+    fac = SyntheticFactors(no, nv, seed)
+    F, ERI, L = fac.hamiltonian()
+    w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
+    ecc = quiet(w.solve_cc, 1e-12, 1e-12, 100, 8, 1)
+    from pycc.cchbar import cchbar
+    from pycc.ccderiv import CCderiv
+    hbar = quiet(cchbar, w)
+    rng = np.random.default_rng(2000 + seed)
+    X1 = 0.1 * rng.standard_normal((no, nv))
+    X2 = 0.1 * rng.standard_normal((no, no, nv, nv))
+    X2 = X2 + X2.transpose(1, 0, 3, 2)
+    host = types.SimpleNamespace(contract=w.contract, ccwfn=w)
+    s1, s2 = CCderiv._ccsd_jacobian(host, X1, X2, hbar)
+    out = {"ecc": float(ecc), "t1": w.t1, "t2": w.t2, "X1": X1, "X2": X2,
+           "sigma1": np.asarray(s1), "sigma2": np.asarray(s2),
+           "sigma2_sym": np.asarray(s2) + np.asarray(s2).transpose(1, 0, 3, 2)}
+    np.savez_compressed(os.path.join(HERE, "o5v19_jacobian.npz"), **out)
+    print("o5v19_jacobian: |sigma1| = %.6e  |sigma2_sym| = %.6e"
+          % (np.linalg.norm(out["sigma1"]), np.linalg.norm(out["sigma2_sym"])))
+
+
 def gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz"):
     """no=20, nv=180, seed 1.  With the spec's plain sigma (coupling 1) CCSD diverges at this
     size, so the converged fixture uses the matched coupling; the raw-sigma fixture keeps the
@@ -228,10 +255,13 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--o20v180", action="store_true")
     ap.add_argument("--no-o5v19", action="store_true")
+    ap.add_argument("--no-jacobian", action="store_true")
     args = ap.parse_args()
     pycc = import_reference()
     if not args.no_o5v19:
         gen_o5v19(pycc)
+    if not args.no_jacobian:
+        gen_o5v19_jacobian(pycc)
     if args.o20v180:
         gen_o20v180(pycc, solve=False, coupling=1.0, name="o20v180_raw.npz")
         gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz")

@@ -1,0 +1,92 @@
+"""Host logic of the FP64 engine and its adjoint on CPU, through the numpy model of the FP64
+entry points (``tests/abi_model.py``): the builders' contraction plans, the residual's tape,
+its forward sweep (the Jacobian action) and reverse sweep (Lambda), the density assembly.
+The kernels themselves are covered by the ``-m gpu`` tests.
+
+* The residual and the converged energy against the reference's (o5v19.npz).
+* J.X against the reference's ``CCderiv._ccsd_jacobian`` at its converged amplitudes
+  (o5v19_jacobian.npz), symmetrised doubles, 1e-12 relative.
+* <l, J x> = <J^T l, x> and dE/dt . x from the two sweeps, to rounding.
+* Lambda + gradient densities against the reference's D and Gamma (8-fold symmetric
+  projection, 1e-9) and the energy identity E = <D,F> + <Gamma,ERI>.
+"""
+import numpy as np
+import pytest
+import torch
+
+import abi_model
+import pycc_gb300 as pg
+from conftest import golden
+from pycc_gb300.adjoint import CCSDAdjoint, symmetrize8
+
+
+@pytest.fixture
+def model(monkeypatch):
+    m = abi_model.install(monkeypatch)
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a, **k: None)
+    return m
+
+
+def rel(a, b):
+    a = a.numpy() if isinstance(a, torch.Tensor) else a
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def wavefunction(ham, t1=None, t2=None):
+    _, F, ERI, L = ham
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu"))
+    if t1 is not None:
+        w.t1 = torch.from_numpy(np.ascontiguousarray(t1))
+        w.t2 = torch.from_numpy(np.ascontiguousarray(t2))
+    return w
+
+
+def test_residual_and_solve(model, ham_o5v19, golden_o5v19):
+    g = golden_o5v19
+    w = wavefunction(ham_o5v19)
+    r1, r2 = w.residuals(w.H.F, torch.from_numpy(g["probe_t1"].copy()),
+                         torch.from_numpy(g["probe_t2"].copy()))
+    assert rel(r1, g["r1"]) < 1e-13 and rel(r2, g["r2"]) < 1e-13
+    e = w.solve_cc(1e-12, 1e-12)
+    assert abs(e - float(g["ecc"])) < 1e-12
+    assert w.niter == len(g["ecc_iters"]) - 1
+
+
+def test_jacobian_vs_reference(model, ham_o5v19):
+    g = golden("o5v19_jacobian.npz")
+    adj = CCSDAdjoint(wavefunction(ham_o5v19, g["t1"], g["t2"]))
+    s1, s2 = adj.jacobian(torch.from_numpy(g["X1"].copy()), torch.from_numpy(g["X2"].copy()))
+    assert rel(s1, g["sigma1"]) < 1e-12
+    assert rel(s2 + s2.permute(1, 0, 3, 2), g["sigma2_sym"]) < 1e-12
+    assert torch.equal(s2, s2.permute(1, 0, 3, 2))          # half of the symmetric action
+    with pytest.raises(ValueError):
+        adj.jacobian(torch.zeros(5, 19), torch.zeros(5, 5, 19, 19))   # float32
+
+
+def test_sweeps_are_transposes(model, ham_o5v19, golden_o5v19):
+    adj = CCSDAdjoint(wavefunction(ham_o5v19, golden_o5v19["t1"], golden_o5v19["t2"]))
+    rng = np.random.default_rng(9)
+    x1, l1 = (torch.from_numpy(rng.standard_normal((5, 19))) for _ in range(2))
+    x2, l2 = (torch.from_numpy(rng.standard_normal((5, 5, 19, 19))) for _ in range(2))
+    dr1, dr2, dE = adj.jvp(x1, x2)
+    lhs = float((l1 * dr1).sum() + (l2 * dr2).sum())
+    G = adj.backward(l1=l1, l2=l2)
+    rhs = float((G.get(adj.t1) * x1).sum() + (G.get(adj.t2) * x2).sum())
+    assert abs(lhs - rhs) < 1e-12 * abs(lhs)
+    G = adj.backward(gE=1.0)
+    ref = float((G.get(adj.t1) * x1).sum() + (G.get(adj.t2) * x2).sum())
+    assert abs(float(dE) - ref) < 1e-12 * abs(ref)
+
+
+def test_lambda_and_densities(model, ham_o5v19, golden_o5v19):
+    g = golden_o5v19
+    _, F, ERI, _ = ham_o5v19
+    w = wavefunction(ham_o5v19)
+    e = w.solve_cc(1e-12, 1e-12)
+    adj = CCSDAdjoint(w)
+    adj.solve_lambda(1e-12, 1e-12, 200)
+    gF, Gam = adj.gradient()
+    assert abs(float((gF.numpy() * F).sum() + (Gam.numpy() * ERI).sum()) - e) < 1e-10
+    D, G = torch.from_numpy(g["D"]), torch.from_numpy(g["Gamma"])
+    assert (0.5 * (gF + gF.T) - 0.5 * (D + D.T)).abs().max().item() < 1e-9
+    assert (symmetrize8(Gam) - symmetrize8(G)).abs().max().item() < 1e-9
