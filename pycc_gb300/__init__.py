@@ -8,9 +8,11 @@ from .hamiltonian import Hamiltonian, BlockTensor
 from .synth import SyntheticFactors, WORKLOADS, synthetic_factors
 from .ccwfn import CCwfn, ccwfn
 from .contract import ContractionBackend, contract_f64
+from .lagrangian import cchbar, cclambda, ccdensity
 
 __all__ = [
     "CCwfn", "ccwfn", "Hamiltonian", "BlockTensor", "SyntheticFactors", "WORKLOADS",
-    "synthetic_factors", "ContractionBackend", "contract_f64", "PyCCError",
+    "synthetic_factors", "ContractionBackend", "contract_f64", "cchbar", "cclambda",
+    "ccdensity", "PyCCError",
     "InvalidKeywordError", "ConvergenceError", "NumericalError",
 ]

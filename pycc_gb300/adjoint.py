@@ -353,12 +353,16 @@ class CCSDAdjoint:
         raise ConvergenceError("Lambda", maxiter, pseudo - pseudo_last, rms)
 
     # -- gradient densities ---------------------------------------------------------------
-    def gradient(self, e_conv=1e-10, r_conv=1e-10, maxiter=100):
-        """dE/dF (nmo x nmo) and dE/d<pq|rs> (nmo^4) at the converged amplitudes."""
-        if not hasattr(self, "l1"):
-            self.solve_lambda(e_conv, r_conv, maxiter)
+    def gradient(self, e_conv=1e-10, r_conv=1e-10, maxiter=100, l1=None, l2=None):
+        """dL/dF (nmo x nmo) and dL/d<pq|rs> (nmo^4) of the Lagrangian L = E + <l, r> at the
+        taped amplitudes: with the converged Lambda amplitudes (solved here when neither
+        (l1, l2) nor an earlier solve gives them) these are dE/dF and dE/d<pq|rs>."""
+        if l1 is None or l2 is None:
+            if not hasattr(self, "l1"):
+                self.solve_lambda(e_conv, r_conv, maxiter)
+            l1, l2 = self.l1, self.l2
         t0 = time.time()
-        G = self.backward(gE=1.0, l1=self.l1, l2=self.l2, wrt_H=True)
+        G = self.backward(gE=1.0, l1=l1, l2=l2, wrt_H=True)
         w = self.w
         H = w.H
         no, nv, n = w.no, w.nv, w.nmo

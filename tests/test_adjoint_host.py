@@ -90,3 +90,42 @@ def test_lambda_and_densities(model, ham_o5v19, golden_o5v19):
     D, G = torch.from_numpy(g["D"]), torch.from_numpy(g["Gamma"])
     assert (0.5 * (gF + gF.T) - 0.5 * (D + D.T)).abs().max().item() < 1e-9
     assert (symmetrize8(Gam) - symmetrize8(G)).abs().max().item() < 1e-9
+
+
+def test_reference_objects_chain(model, ham_o5v19, golden_o5v19):
+    """cchbar -> cclambda -> ccdensity with the reference's constructors, methods and
+    normalisation: pseudo-energy, l1 and l2 against the reference's cclambda, D and Gamma
+    against its ccdensity.gradient_densities (symmetric projections), compute_energy
+    against the converged energy."""
+    g = golden_o5v19
+    w = wavefunction(ham_o5v19)
+    e = w.solve_cc(1e-12, 1e-12)
+    hbar = pg.cchbar(w)
+    with pytest.raises(AttributeError, match="does not materialise"):
+        hbar.Hvvvv
+    lam = pg.cclambda(w, hbar)
+    t1, t2 = g["t1"], g["t2"]
+    assert rel(lam.l1, 2.0 * t1) < 1e-9                                # the reference's guess
+    assert rel(lam.l2, 2.0 * (2.0 * t2 - t2.swapaxes(2, 3))) < 1e-9
+    dens0 = pg.ccdensity(w, lam)                                      # any lambda: L = E at r = 0
+    assert abs(dens0.compute_energy() - e) < 1e-10
+    pseudo = lam.solve_lambda(1e-12, 1e-12, 200)
+    assert abs(pseudo - float(g["lambda_pseudo"])) < 1e-10
+    assert rel(lam.l1, g["l1"]) < 1e-9 and rel(lam.l2, g["l2"]) < 1e-9
+    dens = pg.ccdensity(w, lam)
+    D, G = dens.gradient_densities()
+    Dr, Gr = torch.from_numpy(g["D"]), torch.from_numpy(g["Gamma"])
+    assert (D - 0.5 * (Dr + Dr.T)).abs().max().item() < 1e-9
+    assert (G - symmetrize8(Gr)).abs().max().item() < 1e-9
+    assert abs(dens.compute_energy() - e) < 1e-10
+    assert abs(dens.compute_energy() - float(g["E_from_densities"])) < 1e-10
+    with pytest.raises(RuntimeError):
+        pg.ccdensity(w, lam, onlyone=True).gradient_densities()
+
+
+def test_density_symmetrisation_kernel_path(model):
+    """The eight-fold projection on the combination kernel equals the torch definition."""
+    from pycc_gb300.lagrangian import symmetrize_density2
+    G = torch.from_numpy(np.random.default_rng(3).standard_normal((4, 5, 6, 7))[:, :4, :4, :4]
+                         .copy()).contiguous()
+    assert (symmetrize_density2(G) - symmetrize8(G)).abs().max().item() < 1e-15
