@@ -3,10 +3,12 @@
 Each function restates the documented semantics of one entry point of
 ``include/pycc_gb300.h`` on tensors in host memory (``data_ptr()`` of a CPU tensor is a host
 address).  Tests install it in place of ``pycc_gb300._lib.call`` to run the host code of the
-FP64 engine -- the builders' contraction plans, the adjoint tape and its sweeps, the solver
-loops, DIIS -- without a GPU.  The CUDA kernels themselves are checked against the oracle in
-the ``-m gpu`` tests; nothing here says anything about them, and nothing outside ``tests/``
-imports this module.
+engine -- the builders' contraction plans, the mixed engine's operand definitions and output
+maps, the adjoint tape and its sweeps, the solver loops, DIIS -- without a GPU.  The
+tensor-core pack and GEMM are modelled in exact FP64 (no format rounding), so a residual
+planned by the mixed engine must equal the FP64 residual to rounding.  The CUDA kernels
+themselves are checked against the oracle in the ``-m gpu`` tests; nothing here says anything
+about them, and nothing outside ``tests/`` imports this module.
 """
 from __future__ import annotations
 
@@ -39,6 +41,7 @@ class ABIModel:
 
     def __init__(self):
         self.calls = []
+        self.packs = {}           # hi buffer address -> the FP64 values a pack would convert
 
     def __call__(self, name, *a):
         self.calls.append(name)
@@ -134,6 +137,62 @@ class ABIModel:
         flat(out, n)[...] = acc
 
     lincomb_f64_df = lincomb_f64
+
+    # -- the tensor-core engine, modelled in exact FP64 --------------------------------------
+    # A pack records the FP64 values it would convert (keyed by its hi buffer); the GEMM
+    # multiplies those.  The model so checks which operand combinations, layouts and output
+    # maps the host plans, independently of the GEMM formats' rounding.
+    @staticmethod
+    def _offsets(ext, strides):
+        off = np.zeros(1, dtype=np.int64)
+        for e, s in zip(ext, strides):
+            off = (off[:, None] + np.arange(e, dtype=np.int64)[None, :] * s).ravel()
+        return off
+
+    def pack_operand(self, fmt, r_n, r_ext, r_str, k_n, k_ext, k_str, Kp, a, X, b, Y, c, P, Q,
+                     hi, mid, lo, scale, row_tab, rows, _st):
+        re_, ke = _ints(r_ext, r_n), _ints(k_ext, k_n)
+        rs, ks = _ints(r_str, 16), _ints(k_str, 16)
+        K = int(np.prod(ke)) if ke else 1
+        assert K <= Kp and Kp % (128 if fmt == 2 else 64) == 0
+        if row_tab:
+            tab = flat(row_tab, 4 * rows, np.int64).reshape(4, rows)
+        R = rows if row_tab else (int(np.prod(re_)) if re_ else 1)
+
+        def source(s, ptr):
+            koff = self._offsets(ke, ks[4 * s:4 * s + k_n])
+            roff = tab[s] if row_tab else self._offsets(re_, rs[4 * s:4 * s + r_n])
+            idx = roff[:, None] + koff[None, :]
+            return flat(ptr, int(idx.max()) + 1)[idx]
+
+        v = np.zeros((R, K))
+        if X:
+            v += a * source(0, X)
+        if Y:
+            v += b * source(1, Y)
+        if P:
+            v += c * source(2, P) * source(3, Q)
+        self.packs[hi] = v
+
+    def tc_gemm(self, fmt, A_hi, A_mid, A_lo, M, lda, B_hi, B_mid, B_lo, N, ldb, Kp, a_scale,
+                b_scale, m_n, m_ext, m_sc, n_n, n_ext, n_sc, col_map, col_scale, alpha, beta, Cp,
+                _status, _st):
+        A, B = self.packs[A_hi], self.packs[B_hi]
+        assert A.shape[0] == M and B.shape[0] == N and A.shape[1] == B.shape[1]
+        offm = self._offsets(_ints(m_ext, m_n), _ints(m_sc, m_n))
+        assert offm.size == M
+        if col_map:
+            offn = flat(col_map, N, np.int64).copy()
+        else:
+            offn = self._offsets(_ints(n_ext, n_n), _ints(n_sc, n_n))
+        assert offn.size == N and 0 <= offn.min() and offn.max() < 2 ** 31
+        S = alpha * (A @ B.T)
+        if col_scale:
+            S = S * flat(col_scale, N)[None, :]
+        idx = offm[:, None] + offn[None, :]
+        assert np.unique(idx).size == idx.size, "output map is not injective"
+        Cf = flat(Cp, int(idx.max()) + 1)
+        Cf[idx] = S if beta == 0.0 else beta * Cf[idx] + S
 
 
 def install(monkeypatch):
