@@ -161,10 +161,6 @@ class MixedResidual:
     def ll(self, pat, labels):
         return Operand.of(labels, self.w.H.L.blocks[pat], key=("L", pat))
 
-    @staticmethod
-    def t2op(labels, t2, t2lab=None):
-        return Operand.of(labels, t2) if t2lab is None else Operand(labels, (t2, t2lab))
-
     # -- the <ab|ef> ladder over i <= j pairs (pycc/ccwfn.py:931) ---------------------------
     def _pair_tables(self):
         if self._pairs is None:

@@ -204,9 +204,6 @@ class TCEngine:
         self.timing = None        # list of GEMM launch records (CUDA events) when set
         self.dyn_cache = None     # per-residual cache of packed dynamic operands
 
-    def cached_bytes(self):
-        return sum(p.nbytes() for p in self.cache.values())
-
     def contract(self, subscripts, A: Operand, B: Operand, out, alpha=1.0, beta=1.0, fmt=FMT_BF16):
         lhs, rhs = subscripts.replace(" ", "").split("->")
         la, lb = lhs.split(",")
