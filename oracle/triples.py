@@ -52,31 +52,40 @@ def denom_ijk(o, v, i, j, k, F):
     return fo[i] + fo[j] + fo[k] - fv.reshape(-1, 1, 1) - fv.reshape(-1, 1) - fv
 
 
+def ijk_energy(o, v, i, j, k, W, t1, t2, Voovv, F):
+    """The Lee-Rendell contribution of one triple i >= j >= k (cctriples.py:207-238) from its
+    connected triples W[a,b,c] without denominator: V = (W + t3d) / (1 + d_ab + d_ac + d_bc),
+    the X / Y / Z symmetry intermediates, and the a >= b >= c sum with weight
+    2 - d_ij - d_ik - d_jk."""
+    nv = W.shape[0]
+    a = np.arange(nv)
+    w = 1.0 + (a[:, None, None] == a[None, :, None]) + (a[:, None, None] == a[None, None, :]) \
+        + (a[None, :, None] == a[None, None, :])
+    tri = (a[:, None, None] >= a[None, :, None]) & (a[None, :, None] >= a[None, None, :])
+    V = (t3d_ijk(o, v, i, j, k, t1, t2, Voovv, F) + W) / w
+    tr = lambda X, p: X.transpose(p)
+    perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    X = sum(tr(W, p) * tr(V, p) for p in perms)
+    Y = V + tr(V, (1, 2, 0)) + tr(V, (2, 0, 1))
+    Z = tr(V, (0, 2, 1)) + tr(V, (1, 0, 2)) + tr(V, (2, 1, 0))
+    Wc = W + tr(W, (1, 2, 0)) + tr(W, (2, 0, 1))
+    Wa = tr(W, (0, 2, 1)) + tr(W, (1, 0, 2)) + tr(W, (2, 1, 0))
+    S = (Y - 2 * Z) * Wc + (Z - 2 * Y) * Wa + 3 * X
+    fac = 2.0 - ((i == j) + (i == k) + (j == k))
+    return fac * np.sum((S / denom_ijk(o, v, i, j, k, F))[tri])
+
+
 def t_tjl(no, nv, F, ERI, t1, t2):
     """Lee-Rendell E(T) (cctriples.py:177-240), vectorised over a, b, c."""
     n = no + nv
     o, v = slice(0, no), slice(no, n)
     Vvvvo, Vovoo, Voovv = ERI[v, v, v, o], ERI[o, v, o, o], ERI[o, o, v, v]
-    a = np.arange(nv)
-    w = 1.0 + (a[:, None, None] == a[None, :, None]) + (a[:, None, None] == a[None, None, :]) \
-        + (a[None, :, None] == a[None, None, :])
-    tri = (a[:, None, None] >= a[None, :, None]) & (a[None, :, None] >= a[None, None, :])
     ET = 0.0
     for i in range(no):
         for j in range(i + 1):
             for k in range(j + 1):
                 W = t3c_ijk(o, v, i, j, k, t2, Vvvvo, Vovoo, F, with_denom=False)
-                V = (t3d_ijk(o, v, i, j, k, t1, t2, Voovv, F) + W) / w
-                tr = lambda X, p: X.transpose(p)
-                perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
-                X = sum(tr(W, p) * tr(V, p) for p in perms)
-                Y = V + tr(V, (1, 2, 0)) + tr(V, (2, 0, 1))
-                Z = tr(V, (0, 2, 1)) + tr(V, (1, 0, 2)) + tr(V, (2, 1, 0))
-                Wc = W + tr(W, (1, 2, 0)) + tr(W, (2, 0, 1))
-                Wa = tr(W, (0, 2, 1)) + tr(W, (1, 0, 2)) + tr(W, (2, 1, 0))
-                S = (Y - 2 * Z) * Wc + (Z - 2 * Y) * Wa + 3 * X
-                fac = 2.0 - ((i == j) + (i == k) + (j == k))
-                ET += fac * np.sum((S / denom_ijk(o, v, i, j, k, F))[tri])
+                ET += ijk_energy(o, v, i, j, k, W, t1, t2, Voovv, F)
     return ET
 
 

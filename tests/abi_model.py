@@ -4,7 +4,9 @@ Each function restates the documented semantics of one entry point of
 ``include/pycc_gb300.h`` on tensors in host memory (``data_ptr()`` of a CPU tensor is a host
 address).  Tests install it in place of ``pycc_gb300._lib.call`` to run the host code of the
 engine -- the builders' contraction plans, the mixed engine's operand definitions and output
-maps, the adjoint tape and its sweeps, the solver loops, DIIS -- without a GPU.  The
+maps, the (T) drivers' layouts and batches, the adjoint tape and its sweeps, the solver loops,
+DIIS -- without a GPU.  The (T) energy entry point is modelled with the oracle's per-triple
+Lee-Rendell energy.  The
 tensor-core pack and GEMM are modelled in exact FP64 (no format rounding), so a residual
 planned by the mixed engine must equal the FP64 residual to rounding.  The CUDA kernels
 themselves are checked against the oracle in the ``-m gpu`` tests; nothing here says anything
@@ -195,12 +197,89 @@ class ABIModel:
         Cf[idx] = S if beta == 0.0 else beta * Cf[idx] + S
 
 
+    # -- the (T) entry points ------------------------------------------------------------------
+    PART_LEN = 4              # the model's per-triple partial-sum length in FP32 mode
+
+    def contract_multi_f64(self, nt, m_n, m_ext, m_sc, m_sa, n_n, n_ext, n_sc, n_sb, k_n, k_ext,
+                           k_sa, k_sb, alpha, A, B, beta, Cp, _st):
+        me, ne = _ints(m_ext, m_n), _ints(n_ext, n_n)
+        Cv = view(Cp, me + ne, _ints(m_sc, m_n) + _ints(n_sc, n_n))
+        acc = 0.0
+        for t in range(nt):
+            kn = int(k_n[t])
+            ke = [int(k_ext[4 * t + q]) for q in range(kn)]
+            sa = [int(m_sa[4 * t + q]) for q in range(m_n)] + [int(k_sa[4 * t + q]) for q in range(kn)]
+            sb = [int(n_sb[4 * t + q]) for q in range(n_n)] + [int(k_sb[4 * t + q]) for q in range(kn)]
+            Av, Bv = view(A[t], me + ke, sa), view(B[t], ne + ke, sb)
+            acc = acc + alpha[t] * np.tensordot(Av, Bv, axes=(list(range(m_n, m_n + kn)),
+                                                                list(range(n_n, n_n + kn))))
+        Cv[...] = acc if beta == 0.0 else beta * Cv + acc
+
+    def tc_grouped_gemm(self, na, a_ptr, a_rows, a_ld, nb, b_ptr, b_rows, b_ld, groups, ngroups,
+                        M, N, Cp, ldm, ldn, _status, _st):
+        from pycc_gb300.triples_tc import GROUP_DTYPE
+        g = np.frombuffer((C.c_char * (ngroups * GROUP_DTYPE.itemsize)).from_address(groups),
+                          dtype=GROUP_DTYPE)
+        As = [self.packs[a_ptr[q]] for q in range(na)]
+        Bs = [self.packs[b_ptr[q]] for q in range(nb)]
+        m, n = np.arange(M), np.arange(N)
+        for rec in g:
+            acc = np.zeros((M, N))
+            for s in range(int(rec["nseg"])):
+                A = As[rec["amap"][s]][rec["arow"][s] + m]
+                B = Bs[rec["bmap"][s]][rec["brow"][s] + n]
+                assert A.shape[1] <= 64 * rec["nkb"][s]
+                acc += A @ B.T
+            idx = int(rec["out"]) + m[:, None] * ldm + n[None, :] * ldn
+            flat(Cp, int(idx.max()) + 1, np.float32)[idx] = acc.astype(np.float32)
+
+    def triples_energy(self, fp32, P1, P2, P3, pstride, ijk, ntrip, eps, eoovv, t1, t2, fov,
+                       no, nv, part, _st):
+        from oracle.triples import ijk_energy
+        dt = np.float32 if fp32 else np.float64
+        v3 = nv ** 3
+        tri = flat(ijk, 3 * ntrip, np.int32).reshape(ntrip, 3)
+        e = flat(eps, no + nv)
+        F = np.diag(e)
+        if fov:
+            F[:no, no:] = flat(fov, no * nv).reshape(no, nv)
+        V = flat(eoovv, no * no * nv * nv, dt).astype(np.float64).reshape(no, no, nv, nv)
+        T1 = flat(t1, no * nv).reshape(no, nv)
+        T2 = flat(t2, no * no * nv * nv, dt).astype(np.float64).reshape(no, no, nv, nv)
+        plen = self.PART_LEN if fp32 else nv
+        out = flat(part, ntrip * plen)
+        o, v = slice(0, no), slice(no, no + nv)
+        for t in range(ntrip):
+            # a partial is stored [z][x][y] for the logical P[x, y, z]
+            P = [flat(p + t * pstride * np.dtype(dt).itemsize, v3, dt).astype(np.float64)
+                 .reshape(nv, nv, nv).transpose(1, 2, 0) for p in (P1, P2, P3)]
+            W = P[0] + P[1].transpose(0, 2, 1) + P[2].transpose(2, 0, 1)
+            i, j, k = (int(x) for x in tri[t])
+            out[t * plen:(t + 1) * plen] = 0.0
+            out[t * plen] = ijk_energy(o, v, i, j, k, W, T1, T2, V, F)
+
+    def reduce_sum_f64(self, x, n, out, _st):
+        flat(out, 1)[0] += flat(x, n).sum()
+
+
+class _LibStub:
+    """The two size queries the host makes on the library object itself."""
+
+    @staticmethod
+    def pcg_triples_part_len(fp32, nv):
+        return ABIModel.PART_LEN if fp32 else nv
+
+    @staticmethod
+    def pcg_tc_group_desc_size():
+        return 96
+
+
 def install(monkeypatch):
     """Route the engine's library calls to the model (CPU tensors accepted)."""
     from pycc_gb300 import _lib, contract
     model = ABIModel()
     monkeypatch.setattr(_lib, "call", model)
-    monkeypatch.setattr(_lib, "load", lambda *a, **k: None)
+    monkeypatch.setattr(_lib, "load", lambda *a, **k: _LibStub)
     monkeypatch.setattr(_lib, "stream_handle", lambda stream=None: None)
 
     def check(t, name):

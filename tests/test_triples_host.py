@@ -1,0 +1,61 @@
+"""Host logic of the (T) correction on CPU, through the numpy model of the entry points
+(``tests/abi_model.py``), against the reference's own E(T) (``t_tjl``, o5v19.npz).
+
+* FP64 path: the twelve t3 terms as three multi-term contractions per triple, written in the
+  [z][x][y] partial layout, then the energy entry point -- to 1e-13.
+* Tensor-core path: six operand packs, the group tables of the grouped GEMM (three
+  orientations per triple, four K segments each), partial offsets inside a batch, FP32
+  partials and per-batch reductions -- for batch sizes that divide the 35 triples of no=5
+  and ones that leave a ragged last batch; within the FP32 storage of the partials (1e-9).
+* ``model='CCSD(T)'`` through ``solve_cc`` in DP and MIXED.
+"""
+import numpy as np
+import pytest
+import torch
+
+import abi_model
+import pycc_gb300 as pg
+from pycc_gb300.triples import t_energy_fp64
+from pycc_gb300.triples_tc import t_energy_tc
+
+
+@pytest.fixture
+def model(monkeypatch):
+    m = abi_model.install(monkeypatch)
+    monkeypatch.setattr(torch.cuda.nvtx, "range_push", lambda *a: None)
+    monkeypatch.setattr(torch.cuda.nvtx, "range_pop", lambda *a: None)
+    return m
+
+
+def converged(ham, g, precision="DP", model_name="CCSD"):
+    _, F, ERI, L = ham
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu"), precision=precision,
+                 model=model_name)
+    w.t1 = torch.from_numpy(g["t1"].copy())
+    w.t2 = torch.from_numpy(g["t2"].copy())
+    return w
+
+
+def test_fp64_path(model, ham_o5v19, golden_o5v19):
+    w = converged(ham_o5v19, golden_o5v19)
+    assert abs(t_energy_fp64(w) - float(golden_o5v19["et_tjl"])) < 1e-13
+    assert "pcg_contract_multi_f64" in model.calls
+
+
+@pytest.mark.parametrize("batch", [32, 35, 7, 4, 1])
+def test_tensor_core_path_batches(model, ham_o5v19, golden_o5v19, batch):
+    w = converged(ham_o5v19, golden_o5v19)
+    et = t_energy_tc(w, batch=batch)
+    assert abs(et - float(golden_o5v19["et_tjl"])) < 1e-9
+    assert "pcg_tc_grouped_gemm" in model.calls
+
+
+@pytest.mark.parametrize("precision,tol", [("DP", 1e-11), ("MIXED", 1e-9)])
+def test_ccsd_t_model(model, ham_o5v19, golden_o5v19, precision, tol):
+    _, F, ERI, L = ham_o5v19
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu"), precision=precision,
+                 model="CCSD(T)")
+    e = w.solve_cc(1e-12, 1e-12, 100)
+    g = golden_o5v19
+    assert abs(e - (float(g["ecc"]) + float(g["et_tjl"]))) < tol
+    assert abs(w.et - float(g["et_tjl"])) < tol
