@@ -15,12 +15,15 @@ Conventions of the reference kept here:
   lambda on r2 (the engine pairs lambda with the symmetrised r2); the starting guess
   l1 = 2 t1, l2 = 2 (2 t2 - t2.swapaxes(2,3)) (``pycc/cclambda.py:66-67``);
 * ``solve_lambda(...)`` returns the pseudo-energy 1/2 <ij|ab> l2_ijab (``:547-570``);
+* ``ccdensity.Doo / Dov / Dvo / Dvv`` and the D of ``gradient_densities()`` are the
+  reference's one-particle density, not symmetrised: dL/dF_pq with F a general matrix, which
+  is what the reference's blocks are (``pycc/ccdensity.py:335-470``);
 * ``gradient_densities()`` returns (D, Gamma), nmo^2 and nmo^4 in <pq|rs> order, with
-  E_corr = <D, F> + <Gamma, ERI>.  The reference stores representative blocks and
-  symmetrises Gamma four-fold; a gradient is defined only up to the permutations under which
-  real F and <pq|rs> are symmetric, so D is returned symmetrised and Gamma symmetrised
-  eight-fold.  Both agree with the reference's on those projections, which is all any real
-  symmetric perturbation, and the generalised-Fock contraction, sees.
+  E_corr = <D, F> + <Gamma, ERI>.  The reference stores representative two-particle blocks
+  with per-block factors and symmetrises Gamma four-fold; the energy defines Gamma only up
+  to the eight permutations under which real <pq|rs> are symmetric, so Gamma is returned
+  symmetrised eight-fold.  It agrees with the reference's on that projection, which is all a
+  real symmetric perturbation, and the generalised-Fock contraction, sees.
 """
 from __future__ import annotations
 
@@ -118,6 +121,9 @@ class ccdensity:
         adj = cclambda.hbar.adjoint
         l2 = _combine(0.5, cclambda.l2, 0.0, None, ccwfn.stream)     # the engine's lambda
         self._D, self._Gam = adj.gradient(l1=cclambda.l1, l2=l2)
+        o, v = ccwfn.o, ccwfn.v
+        self.Doo, self.Dov = self._D[o, o], self._D[o, v]
+        self.Dvo, self.Dvv = self._D[v, o], self._D[v, v]
         self.timing = time.time() - t0
 
     def gradient_densities(self):
@@ -125,9 +131,7 @@ class ccdensity:
         if self.onlyone:
             raise RuntimeError("gradient_densities needs the two-particle density "
                                "(construct ccdensity with onlyone=False).")
-        st = self.ccwfn.stream
-        D = _combine(0.5, self._D, 0.5, (0, 1, 3, 2), st)
-        return D, symmetrize_density2(self._Gam, st)
+        return self._D.clone(), symmetrize_density2(self._Gam, self.ccwfn.stream)
 
     def compute_energy(self):
         """The correlation energy from the densities (``pycc/ccdensity.py:113-211``): <D, F>,

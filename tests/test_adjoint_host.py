@@ -115,7 +115,10 @@ def test_reference_objects_chain(model, ham_o5v19, golden_o5v19):
     dens = pg.ccdensity(w, lam)
     D, G = dens.gradient_densities()
     Dr, Gr = torch.from_numpy(g["D"]), torch.from_numpy(g["Gamma"])
-    assert (D - 0.5 * (Dr + Dr.T)).abs().max().item() < 1e-9
+    assert (D - Dr).abs().max().item() < 1e-9                         # not symmetrised
+    o, v = slice(0, 5), slice(5, 24)
+    for blk, s in (("Doo", (o, o)), ("Dov", (o, v)), ("Dvo", (v, o)), ("Dvv", (v, v))):
+        assert (getattr(dens, blk) - Dr[s]).abs().max().item() < 1e-9, blk
     assert (G - symmetrize8(Gr)).abs().max().item() < 1e-9
     assert abs(dens.compute_energy() - e) < 1e-10
     assert abs(dens.compute_energy() - float(g["E_from_densities"])) < 1e-10
