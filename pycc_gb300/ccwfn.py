@@ -145,6 +145,23 @@ class CCwfn:
     def _st(self):
         return _lib.stream_handle(self.stream)
 
+    # -- amplitude checkpoint -------------------------------------------------------------
+    def save_amplitudes(self, path):
+        """Write t1, t2 (FP64) with the sizes and the last converged energy to an ``.npz``
+        file, to restart or warm-start ``solve_cc`` later (``load_amplitudes``)."""
+        np.savez(path, t1=self.t1.cpu().numpy(), t2=self.t2.cpu().numpy(), no=self.no,
+                 nv=self.nv, ecc=np.nan if self.ecc is None else float(self.ecc))
+
+    def load_amplitudes(self, path):
+        """Set t1, t2 from a file written by ``save_amplitudes`` (the sizes must match);
+        ``solve_cc`` then iterates from them instead of the MP2 guess."""
+        with np.load(path, allow_pickle=False) as d:
+            if (int(d["no"]), int(d["nv"])) != (self.no, self.nv):
+                raise ValueError("%s holds amplitudes for no=%d, nv=%d, not no=%d, nv=%d"
+                                 % (path, int(d["no"]), int(d["nv"]), self.no, self.nv))
+            self.t1 = torch.from_numpy(np.asarray(d["t1"], dtype=np.float64)).to(self.device1)
+            self.t2 = torch.from_numpy(np.asarray(d["t2"], dtype=np.float64)).to(self.device1)
+
     def _contract(self, subscripts, *operands, out=None, alpha=1.0, beta=0.0):
         """``self.contract`` (pycc/device.py:64-87) on the FP64 engine; recorded on the
         adjoint tape when one is active."""

@@ -13,6 +13,8 @@ through the engine's own FP64 contraction kernel (setup, outside the iteration).
 """
 from __future__ import annotations
 
+import types
+
 import numpy as np
 import torch
 
@@ -146,6 +148,34 @@ class Hamiltonian:
         del B
         Ft = torch.from_numpy(fac.F.copy()).to(device)
         return cls(Ft, BlockTensor("ERI", no, nv, eri), BlockTensor("L", no, nv, ll), no, nv, device)
+
+    @classmethod
+    def from_npz(cls, path, device="cuda:0"):
+        """A Hamiltonian from an ``.npz`` file, without psi4.  Keys: ``no`` (occupied
+        orbitals), ``F`` (nmo x nmo Fock matrix), and either ``ERI`` (nmo^4, <pq|rs> order as
+        the reference holds it; optionally ``L``) or ``B`` (naux x nmo x nmo, a three-index
+        factor with <pq|rs> = sum_Q B[Q,p,r] B[Q,q,s], built into blocks on the GPU)."""
+        with np.load(path, allow_pickle=False) as d:
+            keys = set(d.files)
+            if not {"no", "F"} <= keys or not ({"ERI", "B"} & keys):
+                raise KeyError("%s: needs 'no', 'F' and one of 'ERI' / 'B' (has %s)"
+                               % (path, sorted(keys)))
+            no = int(d["no"])
+            F = np.asarray(d["F"], dtype=np.float64)
+            n = F.shape[0]
+            if F.shape != (n, n) or not 0 < no < n:
+                raise ValueError("%s: F must be square with 0 < no < nmo" % path)
+            if "B" in keys:
+                B = np.ascontiguousarray(d["B"], dtype=np.float64)
+                if B.ndim != 3 or B.shape[1:] != (n, n):
+                    raise ValueError("%s: B must be naux x nmo x nmo" % path)
+                fac = types.SimpleNamespace(no=no, nv=n - no, B=B, F=F)
+                return cls.from_factors(fac, device=device)
+            ERI = d["ERI"]
+            if ERI.shape != (n,) * 4:
+                raise ValueError("%s: ERI must be nmo^4" % path)
+            L = d["L"] if "L" in keys else None
+            return cls.from_arrays(F, ERI, no, L=L, device=device)
 
     def nbytes(self):
         return self.ERI.nbytes() + self.L.nbytes()

@@ -1,0 +1,57 @@
+"""psi4-free input and the amplitude checkpoint, host logic on CPU through the numpy model of
+the entry points (``tests/abi_model.py``).
+
+* ``Hamiltonian.from_npz`` with the full <pq|rs> (the reference's layout) and with a
+  three-index factor B: the same resident blocks as ``from_arrays``.
+* ``save_amplitudes`` / ``load_amplitudes``: a warm start from converged amplitudes
+  converges at once, to the reference's energy; mismatched sizes are refused.
+"""
+import numpy as np
+import pytest
+import torch
+
+import abi_model
+import pycc_gb300 as pg
+
+
+@pytest.fixture
+def model(monkeypatch):
+    return abi_model.install(monkeypatch)
+
+
+def test_hamiltonian_from_npz(model, tmp_path, ham_o5v19):
+    fac, F, ERI, L = ham_o5v19
+    ref = pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu")
+    np.savez(tmp_path / "full.npz", no=5, F=F, ERI=ERI)
+    np.savez(tmp_path / "fac.npz", no=5, F=F, B=fac.B)
+    for name in ("full.npz", "fac.npz"):
+        H = pg.Hamiltonian.from_npz(tmp_path / name, device="cpu")
+        assert torch.equal(H.F, ref.F)
+        for X, Y in ((H.ERI, ref.ERI), (H.L, ref.L)):
+            for pat, blk in Y.blocks.items():
+                assert (X.blocks[pat] - blk).abs().max().item() < 1e-14, (name, pat)
+    np.savez(tmp_path / "bad.npz", no=5, F=F)
+    with pytest.raises(KeyError):
+        pg.Hamiltonian.from_npz(tmp_path / "bad.npz", device="cpu")
+    np.savez(tmp_path / "bad2.npz", no=5, F=F, B=fac.B[:, :3])
+    with pytest.raises(ValueError):
+        pg.Hamiltonian.from_npz(tmp_path / "bad2.npz", device="cpu")
+
+
+def test_amplitude_checkpoint_warm_start(model, tmp_path, ham_o5v19, golden_o5v19):
+    _, F, ERI, L = ham_o5v19
+    H = pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu")
+    w = pg.CCwfn(H)
+    e = w.solve_cc(1e-12, 1e-12)
+    path = tmp_path / "amps.npz"
+    w.save_amplitudes(path)
+    w2 = pg.CCwfn(H)
+    w2.load_amplitudes(path)
+    assert torch.equal(w2.t2, w.t2) and torch.equal(w2.t1, w.t1)
+    e2 = w2.solve_cc(1e-10, 1e-10)
+    assert w2.niter <= 2 and abs(e2 - float(golden_o5v19["ecc"])) < 1e-11
+    fac = pg.SyntheticFactors(4, 19, 0)
+    F4, ERI4, L4 = fac.hamiltonian()
+    w3 = pg.CCwfn(pg.Hamiltonian.from_arrays(F4, ERI4, 4, L=L4, device="cpu"))
+    with pytest.raises(ValueError, match="no=5"):
+        w3.load_amplitudes(path)
