@@ -14,7 +14,7 @@ Usage::
 
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian]
 
-Config 2 (no=20, nv=180) needs ~30 GB of host RAM and several minutes.
+The no=20, nv=180 fixtures need ~30 GB of host RAM and several minutes.
 """
 from __future__ import annotations
 
