@@ -99,12 +99,36 @@ def _inverse(perm):
     return tuple(inv)
 
 
-class CCSDAdjoint:
-    """Tape of the FP64 residual + energy at the amplitudes of a converged ``CCwfn``."""
+TC_MIN_FLOPS = 1 << 26     # M*N*K from which a sweep's contraction goes to the tensor cores
 
-    def __init__(self, w):
+
+class CCSDAdjoint:
+    """Tape of the FP64 residual + energy at the amplitudes of a converged ``CCwfn``.
+
+    ``sweep`` selects the engine of the sweeps' contractions: ``'fp64'`` (the FP64 DMMA
+    kernel; the default for ``precision='DP'``) or ``'tc'`` (GEMM-shaped contractions of at
+    least ``TC_MIN_FLOPS`` multiply-adds on the tensor cores in split-BF16x3 with separate
+    accumulators, the integral blocks as cached static packs; the default for 'MIXED' and
+    'SP').  The tape is always recorded from the FP64 residual; for a MIXED / SP wave function
+    a DP twin sharing its Hamiltonian and amplitudes records it.
+    """
+
+    def __init__(self, w, sweep=None):
+        if sweep is None:
+            sweep = 'fp64' if w.precision == 'DP' else 'tc'
+        if sweep not in ('fp64', 'tc'):
+            raise ValueError("sweep must be 'fp64' or 'tc', got %r" % (sweep,))
         if w.precision != 'DP':
-            raise ValueError("the adjoint runs on the FP64 path (precision='DP')")
+            from .ccwfn import CCwfn
+            twin = CCwfn(w.H, precision='DP')
+            twin.t1, twin.t2 = w.t1, w.t2
+            w = twin
+        self.sweep = sweep
+        self.tc_min_flops = TC_MIN_FLOPS
+        self._tc = None
+        if sweep == 'tc':
+            from .tc import TCEngine
+            self._tc = TCEngine(w.device1, w.stream)
         self.w = w
         self.stream = w.stream
         H = w.H
@@ -124,6 +148,38 @@ class CCSDAdjoint:
         self.wrt_H = False
         self._work = torch.empty(WORK_LEN, dtype=torch.float64, device=H.F.device)
         self._scal = torch.zeros(4, dtype=torch.float64, device=H.F.device)
+
+    # -- the sweeps' contractions ----------------------------------------------------------
+    def _mm(self, subs, A, B, out, alpha, beta):
+        """out = beta*out + alpha*einsum(subs, A, B): on the tensor cores for a 'tc' sweep and a
+        GEMM-shaped contraction (an output index, none in both operands and the output,
+        K >= 64) of at least ``tc_min_flops`` multiply-adds, else on the FP64 kernel."""
+        if self._tc is not None:
+            lhs, rhs = subs.replace(" ", "").split("->")
+            la, lb = lhs.split(",")
+            ext = dict(zip(la, A.shape))
+            ext.update(zip(lb, B.shape))
+            M = math.prod(ext[c] for c in la if c in rhs)
+            N = math.prod(ext[c] for c in lb if c in rhs)
+            K = math.prod(ext[c] for c in la if c in lb)
+            if (rhs and not (set(la) & set(lb) & set(rhs)) and K >= 64
+                    and M * N * K >= self.tc_min_flops):
+                from .tc import FMT_BF16X3S, Operand
+                opA = Operand(la, (A, la), key=self._static_key(A))
+                opB = Operand(lb, (B, lb), key=self._static_key(B))
+                self._tc.contract(subs, opA, opB, out, alpha=alpha, beta=beta, fmt=FMT_BF16X3S)
+                return
+        contract_f64(subs, A, B, out=out, alpha=alpha, beta=beta, stream=self.stream)
+
+    def _static_key(self, t):
+        """Integral blocks (and views of them) are packed once per sweep engine."""
+        if _key(t) in self.leaves_H:
+            return ("H", t.data_ptr(), tuple(t.shape), tuple(t.stride()))
+        return None
+
+    def _check_tc(self):
+        if self._tc is not None:
+            self._tc.check_status()
 
     # -- reverse accumulation -------------------------------------------------------------
     def _want(self, t):
@@ -150,6 +206,7 @@ class CCSDAdjoint:
             accumulate(G.get(self.r2), l2, stream=st)
         for kind, args in reversed(self.tape.ops):
             getattr(self, "_bw_" + kind)(*args)
+        self._check_tc()
         return G
 
     def _bw_contract(self, subs, A, B, out, alpha, beta):
@@ -160,11 +217,9 @@ class CCSDAdjoint:
         lhs, rhs = subs.replace(" ", "").split("->")
         la, lb = lhs.split(",")
         if self._want(A):
-            contract_f64("%s,%s->%s" % (rhs, lb, la), gZ, B, out=G.get(A), alpha=alpha, beta=1.0,
-                         stream=self.stream)
+            self._mm("%s,%s->%s" % (rhs, lb, la), gZ, B, G.get(A), alpha, 1.0)
         if self._want(B):
-            contract_f64("%s,%s->%s" % (la, rhs, lb), A, gZ, out=G.get(B), alpha=alpha, beta=1.0,
-                         stream=self.stream)
+            self._mm("%s,%s->%s" % (la, rhs, lb), A, gZ, G.get(B), alpha, 1.0)
 
     def _bw_copy(self, X, out):
         G = self.grads
@@ -190,8 +245,8 @@ class CCSDAdjoint:
             accumulate(G.get(t2), gO, f1, stream=self.stream)
         if f2 != 0.0:
             g1 = G.get(t1)
-            contract_f64("ijab,jb->ia", gO, t1, out=g1, alpha=f2, beta=1.0, stream=self.stream)
-            contract_f64("ijab,ia->jb", gO, t1, out=g1, alpha=f2, beta=1.0, stream=self.stream)
+            self._mm("ijab,jb->ia", gO, t1, g1, f2, 1.0)
+            self._mm("ijab,ia->jb", gO, t1, g1, f2, 1.0)
 
     def _bw_sym(self, h, out):
         G = self.grads
@@ -220,6 +275,7 @@ class CCSDAdjoint:
         accumulate(T.get(self.t2), x2, stream=self.stream)
         for kind, args in self.tape.ops:
             getattr(self, "_fw_" + kind)(T, *args)
+        self._check_tc()
         return T
 
     def _fw_contract(self, T, subs, A, B, out, alpha, beta):
@@ -230,10 +286,10 @@ class CCSDAdjoint:
         to = T.get(out)
         b = beta                      # 0 for a fresh output: the first term writes it
         if ta is not None:
-            contract_f64(subs, ta, B, out=to, alpha=alpha, beta=b, stream=self.stream)
+            self._mm(subs, ta, B, to, alpha, b)
             b = 1.0
         if tb is not None:
-            contract_f64(subs, A, tb, out=to, alpha=alpha, beta=b, stream=self.stream)
+            self._mm(subs, A, tb, to, alpha, b)
 
     def _fw_copy(self, T, X, out):
         if T.has(X):

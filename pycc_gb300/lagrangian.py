@@ -60,13 +60,14 @@ class cchbar:
     """HBAR of the FP64 engine, represented by the residual's tape (``pycc/cchbar.py:54``).
 
     The reference's blocks (``Hov``, ``Hvvvv``, ...) are not materialised; ``jacobian`` is
-    HBAR's action on an amplitude pair (``CCderiv._ccsd_jacobian``)."""
+    HBAR's action on an amplitude pair (``CCderiv._ccsd_jacobian``).  ``sweep`` ('fp64' or
+    'tc') selects the engine of the tape's sweeps (see :class:`CCSDAdjoint`)."""
 
-    def __init__(self, ccwfn):
+    def __init__(self, ccwfn, sweep=None):
         t0 = time.time()
         self.ccwfn = ccwfn
         self.contract = ccwfn.contract
-        self.adjoint = CCSDAdjoint(ccwfn)
+        self.adjoint = CCSDAdjoint(ccwfn, sweep=sweep)
         self.timing = time.time() - t0
 
     def jacobian(self, X1, X2):

@@ -132,3 +132,46 @@ def test_density_symmetrisation_kernel_path(model):
     G = torch.from_numpy(np.random.default_rng(3).standard_normal((4, 5, 6, 7))[:, :4, :4, :4]
                          .copy()).contiguous()
     assert (symmetrize_density2(G) - symmetrize8(G)).abs().max().item() < 1e-15
+
+
+def test_tensor_core_sweeps(model, ham_o5v19, golden_o5v19):
+    """The 'tc' sweep engine (every GEMM-shaped contraction of the sweeps on the tensor-core
+    engine, here with no size floor) plans the same products as the FP64 sweeps: with the
+    pack and GEMM modelled exactly, J^T l, J x, Lambda and the densities agree to rounding."""
+    g = golden_o5v19
+    w = wavefunction(ham_o5v19, g["t1"], g["t2"])
+    ref = CCSDAdjoint(w, sweep="fp64")
+    tc = CCSDAdjoint(w, sweep="tc")
+    tc.tc_min_flops = 0
+    rng = np.random.default_rng(5)
+    x1, l1 = (torch.from_numpy(rng.standard_normal((5, 19))) for _ in range(2))
+    x2, l2 = (torch.from_numpy(rng.standard_normal((5, 5, 19, 19))) for _ in range(2))
+    n0 = model.calls.count("pcg_tc_gemm")
+    for a, b in zip(ref.jvp(x1, x2), tc.jvp(x1, x2)):
+        assert (a - b).abs().max().item() <= 1e-12 * a.abs().max().item()
+    Ga = [ref.backward(l1=l1, l2=l2).get(t).clone() for t in (ref.t1, ref.t2)]
+    Gb = [tc.backward(l1=l1, l2=l2).get(t).clone() for t in (tc.t1, tc.t2)]
+    for a, b in zip(Ga, Gb):
+        assert (a - b).abs().max().item() <= 1e-12 * a.abs().max().item()
+    assert model.calls.count("pcg_tc_gemm") - n0 > 20
+    lam = pg.cclambda(w, pg.cchbar(w, sweep="tc"))
+    lam.hbar.adjoint.tc_min_flops = 0
+    assert abs(lam.solve_lambda(1e-12, 1e-12, 200) - float(g["lambda_pseudo"])) < 1e-10
+    D, G = pg.ccdensity(w, lam).gradient_densities()
+    assert (D - torch.from_numpy(g["D"])).abs().max().item() < 1e-9
+    assert (G - symmetrize8(torch.from_numpy(g["Gamma"]))).abs().max().item() < 1e-9
+
+
+def test_mixed_wavefunction_gets_a_dp_tape(model, ham_o5v19, golden_o5v19):
+    """A MIXED wave function: the tape is recorded by a DP twin sharing its Hamiltonian and
+    amplitudes, and the sweeps default to the tensor cores."""
+    g = golden_o5v19
+    _, F, ERI, L = ham_o5v19
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu"), precision="MIXED")
+    w.t1 = torch.from_numpy(g["t1"].copy())
+    w.t2 = torch.from_numpy(g["t2"].copy())
+    hbar = pg.cchbar(w)
+    assert hbar.adjoint.sweep == "tc" and hbar.adjoint.w is not w
+    assert hbar.adjoint.w.H is w.H and torch.equal(hbar.adjoint.t2, w.t2)
+    lam = pg.cclambda(w, hbar)
+    assert abs(lam.solve_lambda(1e-12, 1e-12, 200) - float(g["lambda_pseudo"])) < 1e-10
