@@ -153,7 +153,8 @@ class CCSDAdjoint:
     def _mm(self, subs, A, B, out, alpha, beta):
         """out = beta*out + alpha*einsum(subs, A, B): on the tensor cores for a 'tc' sweep and a
         GEMM-shaped contraction (an output index, none in both operands and the output,
-        K >= 64) of at least ``tc_min_flops`` multiply-adds, else on the FP64 kernel."""
+        K >= 64) of at least ``tc_min_flops`` multiply-adds whose output offsets stay below
+        2^31 (the tensor-core epilogue's column offsets are 32-bit), else on the FP64 kernel."""
         if self._tc is not None:
             lhs, rhs = subs.replace(" ", "").split("->")
             la, lb = lhs.split(",")
@@ -162,8 +163,9 @@ class CCSDAdjoint:
             M = math.prod(ext[c] for c in la if c in rhs)
             N = math.prod(ext[c] for c in lb if c in rhs)
             K = math.prod(ext[c] for c in la if c in lb)
+            span = sum((e - 1) * st for e, st in zip(out.shape, out.stride()))
             if (rhs and not (set(la) & set(lb) & set(rhs)) and K >= 64
-                    and M * N * K >= self.tc_min_flops):
+                    and M * N * K >= self.tc_min_flops and span < 2 ** 31):
                 from .tc import FMT_BF16X3S, Operand
                 opA = Operand(la, (A, la), key=self._static_key(A))
                 opB = Operand(lb, (B, lb), key=self._static_key(B))
