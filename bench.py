@@ -267,7 +267,8 @@ def term_mode(args, dev):
 
 def adjoint_mode(args, dev, directions=16):
     """Adjoint at no=20, nv=180 (seed 3, matched coupling): Lambda + gradient densities,
-    backward/forward cost, central finite differences along random symmetric directions."""
+    backward/forward cost, central finite differences along random symmetric directions;
+    the tape's sweeps on the engine ``--adjoint-sweep`` names."""
     import numpy as np
     import torch
     import pycc_gb300 as pg
@@ -281,7 +282,7 @@ def adjoint_mode(args, dev, directions=16):
     fwd = float(np.mean(w.iter_times[1:]))
     torch.cuda.synchronize()
     t0 = time.time()
-    adj = CCSDAdjoint(w)
+    adj = CCSDAdjoint(w, sweep=args.adjoint_sweep)
     adj.solve_lambda(1e-12, 1e-12, 200)
     gF, Gam = adj.gradient()
     torch.cuda.synchronize()
@@ -315,7 +316,8 @@ def adjoint_mode(args, dev, directions=16):
         rows.append({"fd": fd, "adjoint": an, "abs": abs(fd - an), "rel": abs(fd - an) / abs(an)})
         del dE, dF
         torch.cuda.empty_cache()
-    line = {"mode": "adjoint", "config": {"no": no, "nv": nv, "seed": seed, "coupling": "matched"},
+    line = {"mode": "adjoint", "sweep": args.adjoint_sweep,
+            "config": {"no": no, "nv": nv, "seed": seed, "coupling": "matched"},
             "ecc": e, "forward_iter_s": fwd, "forward_niter": w.niter,
             "lambda_niter": adj.lambda_niter,
             "lambda_iter_s": float(np.mean(adj.lambda_times[1:])),
@@ -350,6 +352,8 @@ def main():
                          "contraction (--term) alone at --no/--nv")
     ap.add_argument("--triples-size", type=int, nargs=3, default=None, metavar=("NO", "NV", "SEED"),
                     help="(T) mode at another size (profiling; the measurement is no=30,nv=240)")
+    ap.add_argument("--adjoint-sweep", default="fp64", choices=["fp64", "tc"],
+                    help="adjoint mode: engine of the tape's sweeps (FP64 DMMA or tensor cores)")
     ap.add_argument("--term", default="nb,mnej->mbej")
     ap.add_argument("--term-fmt", default="bf16x3f", choices=["bf16", "bf16x3", "bf16x3f"])
     args = ap.parse_args()
