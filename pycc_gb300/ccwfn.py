@@ -119,6 +119,7 @@ class CCwfn:
                                  device=self.device1)
         self.t2.copy_(H.ERI[self.o, self.o, self.v, self.v] / self.Dijab)
         self._mixed = None
+        self._warm_start = False  # set by load_amplitudes
         self.ecc = None
         self.niter = 0
         self.timing = {"init": time.time() - time_init}
@@ -154,13 +155,16 @@ class CCwfn:
 
     def load_amplitudes(self, path):
         """Set t1, t2 from a file written by ``save_amplitudes`` (the sizes must match);
-        ``solve_cc`` then iterates from them instead of the MP2 guess."""
+        ``solve_cc`` then iterates from them instead of the MP2 guess.  In MIXED / SP the
+        next solve starts in the final precision stage: the fast stages' rounding would only
+        move converged amplitudes away."""
         with np.load(path, allow_pickle=False) as d:
             if (int(d["no"]), int(d["nv"])) != (self.no, self.nv):
                 raise ValueError("%s holds amplitudes for no=%d, nv=%d, not no=%d, nv=%d"
                                  % (path, int(d["no"]), int(d["nv"]), self.no, self.nv))
             self.t1 = torch.from_numpy(np.asarray(d["t1"], dtype=np.float64)).to(self.device1)
             self.t2 = torch.from_numpy(np.asarray(d["t2"], dtype=np.float64)).to(self.device1)
+        self._warm_start = True
 
     def _contract(self, subscripts, *operands, out=None, alpha=1.0, beta=0.0):
         """``self.contract`` (pycc/device.py:64-87) on the FP64 engine; recorded on the
@@ -400,6 +404,9 @@ class CCwfn:
         # the mixed solver's residual carries ~2^-17 relative rounding: FP32 error vectors
         # hold its updates to better than that, at half the bytes
         edt = torch.float32 if self.precision == 'MIXED' else torch.float64
+        if self._warm_start and self.precision != 'DP':
+            self.mixed_engine().force_final()
+        self._warm_start = False
         return DIIS(self._amps, max_diis, self.stream, error_dtype=edt)
 
     def iterate(self, diis, niter, start_diis=1, extrapolate=True):

@@ -55,3 +55,20 @@ def test_amplitude_checkpoint_warm_start(model, tmp_path, ham_o5v19, golden_o5v1
     w3 = pg.CCwfn(pg.Hamiltonian.from_arrays(F4, ERI4, 4, L=L4, device="cpu"))
     with pytest.raises(ValueError, match="no=5"):
         w3.load_amplitudes(path)
+
+
+def test_mixed_warm_start_runs_the_final_stage(model, tmp_path, ham_o5v19, golden_o5v19,
+                                               monkeypatch):
+    monkeypatch.setattr(torch.cuda.nvtx, "range_push", lambda *a: None)
+    monkeypatch.setattr(torch.cuda.nvtx, "range_pop", lambda *a: None)
+    _, F, ERI, L = ham_o5v19
+    H = pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu")
+    w = pg.CCwfn(H)
+    w.solve_cc(1e-12, 1e-12)
+    path = tmp_path / "amps.npz"
+    w.save_amplitudes(path)
+    m = pg.CCwfn(H, precision="MIXED")
+    m.load_amplitudes(path)
+    e = m.solve_cc(1e-10, 1e-10)
+    assert m.mixed_engine().history[0] == "bf16x3s"
+    assert m.niter <= 2 and abs(e - float(golden_o5v19["ecc"])) < 1e-11
