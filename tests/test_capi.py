@@ -50,3 +50,20 @@ def test_argument_errors_without_gpu(lib):
     rc = lib.pcg_dots_f64(None, None, 0, 10, None, 0, None, None)
     assert rc != 0
     assert b"k=0" in lib.pcg_last_error()
+
+
+def test_entry_point_model_matches_the_abi():
+    """The CPU tests' numpy model of the entry points (tests/abi_model.py) takes the same
+    arguments as each entry point's ctypes signature, so host-logic tests call it exactly
+    as they would call the library."""
+    import inspect
+    import abi_model
+    modelled = 0
+    for name, (_res, argtypes) in _lib.SIGNATURES.items():
+        fn = getattr(abi_model.ABIModel, name[4:], None)
+        if fn is None:
+            continue
+        params = list(inspect.signature(fn).parameters)[1:]        # drop self
+        assert len(params) == len(argtypes), (name, len(params), len(argtypes))
+        modelled += 1
+    assert modelled >= 15
