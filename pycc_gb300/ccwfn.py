@@ -87,6 +87,7 @@ class CCwfn:
         if local is not None:
             raise NotImplementedError("local correlation is not part of the GPU engine")
         self.local = None
+        self._reference_options(kwargs)
         if kwargs:
             raise PyCCError("Unknown keyword argument(s): %s" % ", ".join(sorted(kwargs)))
 
@@ -123,6 +124,37 @@ class CCwfn:
         self.ecc = None
         self.niter = 0
         self.timing = {"init": time.time() - time_init}
+
+    def _reference_options(self, kwargs):
+        """The reference's other constructor options (``pycc/ccwfn.py:76-160``,
+        ``pycc/wavefunction.py:111-160``), validated as it validates them.  Options whose
+        default leaves the RHF-CCSD path unchanged are accepted; switching on a feature
+        outside that path raises NotImplementedError."""
+        if 'frozen_core' in kwargs:
+            raise TypeError("the 'frozen_core' argument was removed; the frozen core is taken "
+                            "from the SCF reference")
+        for name, what in (('make_t3_density', "(T) densities"),
+                           ('store_triples', "stored CC3 triples"),
+                           ('field', "a finite field"),
+                           ('real_time', "real-time (complex) amplitudes"),
+                           ('localize_occ', "localised occupied orbitals")):
+            if kwargs.pop(name, False):
+                raise NotImplementedError("%s=True: %s are not part of the GPU engine"
+                                          % (name, what))
+        self.field_strength = kwargs.pop('field_strength', 0.0)
+        self.field_axis = kwargs.pop('field_axis', 'Z')
+        self.local_cutoff = kwargs.pop('local_cutoff', 1e-5)
+        for name, default, valid in (('it2_opt', True, [True, False]),
+                                     ('filter', False, [True, False])):
+            val = kwargs.pop(name, default)
+            if val not in valid:
+                raise InvalidKeywordError(name, val, valid)
+            setattr(self, name, val)
+        local_mos = str(kwargs.pop('local_mos', 'PIPEK_MEZEY')).upper()
+        if local_mos not in ('PIPEK_MEZEY', 'BOYS'):
+            raise InvalidKeywordError('local_mos', local_mos, ['PIPEK_MEZEY', 'BOYS'])
+        self.local_mos = local_mos
+        self.make_t3_density = self.store_triples = self.field = self.real_time = False
 
     # -- amplitude views ------------------------------------------------------------------
     @property

@@ -72,3 +72,28 @@ def test_mixed_warm_start_runs_the_final_stage(model, tmp_path, ham_o5v19, golde
     e = m.solve_cc(1e-10, 1e-10)
     assert m.mixed_engine().history[0] == "bf16x3s"
     assert m.niter <= 2 and abs(e - float(golden_o5v19["ecc"])) < 1e-11
+
+
+def test_reference_constructor_options(model, ham_o5v19):
+    """The reference's constructor options: accepted at their defaults, validated like the
+    reference validates them, refused when they switch on a feature outside the path."""
+    _, F, ERI, L = ham_o5v19
+    H = pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu")
+    w = pg.CCwfn(H, model="ccsd", device="gpu", precision="dp", make_t3_density=False,
+                 store_triples=False, field=False, field_strength=0.0, field_axis="Z",
+                 real_time=False, local=None, local_cutoff=1e-5, it2_opt=True, filter=False,
+                 localize_occ=False, local_mos="boys", orbital_basis="spatial", quiet=True)
+    assert w.model == "CCSD" and w.local_mos == "BOYS" and w.make_t3_density is False
+    for kw in ({"make_t3_density": True}, {"field": True}, {"real_time": True},
+               {"store_triples": True}, {"localize_occ": True}, {"local": "PNO"},
+               {"model": "CC3"}, {"orbital_basis": "spinorbital"}, {"device": "CPU"}):
+        with pytest.raises(NotImplementedError):
+            pg.CCwfn(H, **kw)
+    for kw in ({"it2_opt": 3}, {"local_mos": "EDMISTON"}, {"precision": "HP"},
+               {"model": "CCSDT"}):
+        with pytest.raises(pg.InvalidKeywordError):
+            pg.CCwfn(H, **kw)
+    with pytest.raises(TypeError):
+        pg.CCwfn(H, frozen_core=True)
+    with pytest.raises(pg.PyCCError):
+        pg.CCwfn(H, no_such_option=1)
