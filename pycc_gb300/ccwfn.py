@@ -490,6 +490,9 @@ class CCwfn:
         diis = self.start_iterations(max_diis)
         ecc = self.energies[0]
         ediff, rms = -ecc, float('inf')
+        if not self.quiet:
+            print("iter  %20s  %12s  %12s  %10s  %s" % ("E_corr", "dE", "rms", "time", "precision"))
+            print("%4d  %20.15f  %12.3e" % (0, ecc, -ecc))
         for niter in range(1, maxiter + 1):
             ecc_last = ecc
             ecc, rms = self.iterate(diis, niter, start_diis)
@@ -497,7 +500,9 @@ class CCwfn:
             if callback is not None:
                 callback(niter, ecc, ediff, rms)
             if not self.quiet:
-                print("%4d  %20.15f  %12.3e  %12.3e" % (niter, ecc, ediff, rms))
+                stage = self.mixed_engine().mode_name() if self.precision != 'DP' else 'fp64'
+                print("%4d  %20.15f  %12.3e  %12.3e  %8.3f s  %s"
+                      % (niter, ecc, ediff, rms, self.iter_times[-1], stage))
             done = abs(ediff) < e_conv and rms < r_conv
             if self.precision != 'DP':
                 eng = self.mixed_engine()
