@@ -263,7 +263,7 @@ class MixedResidual:
     # -- residuals (pycc/ccwfn.py:718-945) ------------------------------------------------
     def r_T1(self, F, t1, t2, Fae, Fme, Fmi):
         o, v = self.w.o, self.w.v
-        r = F[v, o].transpose(0, 1).contiguous()
+        r = self.w._copy(F[v, o].transpose(0, 1))   # a fresh tensor, whatever F's layout
         contract_f64('ie,ae->ia', t1, Fae, out=r, beta=1.0)
         contract_f64('mi,ma->ia', Fmi, t1, out=r, alpha=-1.0, beta=1.0)
         t2s = Operand('imae', (t2, 'imae'), a=2.0, Y=(t2, 'imea'), b=-1.0)
