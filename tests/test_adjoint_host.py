@@ -175,3 +175,34 @@ def test_mixed_wavefunction_gets_a_dp_tape(model, ham_o5v19, golden_o5v19):
     assert hbar.adjoint.w.H is w.H and torch.equal(hbar.adjoint.t2, w.t2)
     lam = pg.cclambda(w, hbar)
     assert abs(lam.solve_lambda(1e-12, 1e-12, 200) - float(g["lambda_pseudo"])) < 1e-10
+
+
+@pytest.mark.parametrize("no,nv", [(1, 1), (2, 1), (1, 4), (3, 2)])
+@pytest.mark.parametrize("sweep", ["fp64", "tc"])
+def test_degenerate_sizes(model, no, nv, sweep):
+    """Single occupied or virtual orbitals: J x against a five-point stencil of the residual
+    (exact for the quartic map) and <l, J x> = <J^T l, x>, on both sweep engines."""
+    fac = pg.SyntheticFactors(no, nv, 5)
+    F, ERI, L = fac.hamiltonian()
+    rng = np.random.default_rng(no * 7 + nv)
+    t1 = torch.from_numpy(0.05 * rng.standard_normal((no, nv)))
+    t2 = 0.05 * rng.standard_normal((no, no, nv, nv))
+    t2 = torch.from_numpy(t2 + t2.transpose(1, 0, 3, 2))
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, no, L=L, device="cpu"))
+    w.t1, w.t2 = t1, t2
+    adj = CCSDAdjoint(w, sweep=sweep)
+    adj.tc_min_flops = 0
+    x1, l1 = (torch.from_numpy(rng.standard_normal((no, nv))) for _ in range(2))
+    x2, l2 = (torch.from_numpy(rng.standard_normal((no, no, nv, nv))) for _ in range(2))
+    dr1, dr2, _ = adj.jvp(x1, x2)
+
+    def r(e):
+        return w.residuals(w.H.F, t1 + e * x1, t2 + e * x2)
+    rp, rm, rp2, rm2 = r(1.0), r(-1.0), r(2.0), r(-2.0)
+    for k, d in ((0, dr1), (1, dr2)):
+        fd = (8 * (rp[k] - rm[k]) - (rp2[k] - rm2[k])) / 12
+        assert (fd - d).abs().max().item() <= 1e-10 * max(1.0, fd.abs().max().item())
+    G = adj.backward(l1=l1, l2=l2)
+    lhs = float((l1 * dr1).sum() + (l2 * dr2).sum())
+    rhs = float((G.get(adj.t1) * x1).sum() + (G.get(adj.t2) * x2).sum())
+    assert abs(lhs - rhs) <= 1e-11 * max(1.0, abs(lhs))

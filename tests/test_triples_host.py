@@ -59,3 +59,21 @@ def test_ccsd_t_model(model, ham_o5v19, golden_o5v19, precision, tol):
     g = golden_o5v19
     assert abs(e - (float(g["ecc"]) + float(g["et_tjl"]))) < tol
     assert abs(w.et - float(g["et_tjl"])) < tol
+
+
+@pytest.mark.parametrize("no,nv", [(1, 1), (2, 1), (1, 5), (3, 2)])
+def test_degenerate_sizes(model, no, nv):
+    """Single occupied or virtual orbitals, both drivers, against the oracle's t_tjl."""
+    from oracle import triples as ot
+    fac = pg.SyntheticFactors(no, nv, 5)
+    F, ERI, L = fac.hamiltonian()
+    rng = np.random.default_rng(no * 7 + nv)
+    t1 = 0.05 * rng.standard_normal((no, nv))
+    t2 = 0.05 * rng.standard_normal((no, no, nv, nv))
+    t2 = t2 + t2.transpose(1, 0, 3, 2)
+    ref = ot.t_tjl(no, nv, F, ERI, t1, t2)
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, no, L=L, device="cpu"))
+    w.t1, w.t2 = torch.from_numpy(t1), torch.from_numpy(t2)
+    assert abs(t_energy_fp64(w) - ref) < 1e-13 * max(1.0, abs(ref))
+    for batch in (1, 32):
+        assert abs(t_energy_tc(w, batch=batch) - ref) < 1e-6 * max(abs(ref), 1e-8)
