@@ -1,4 +1,5 @@
 """Host logic of the GPU einsum engine: index classification and sub-index merging."""
+import numpy as np
 import pytest
 import torch
 
@@ -83,3 +84,41 @@ def test_all_residual_subscripts_plan():
         out = torch.empty(p.shape, dtype=torch.float64)
         M, N, K, batch, *_ = p.groups(A, B, out)
         assert not batch and max(len(M), len(N), len(K)) <= 4, subs
+
+
+def test_random_contractions_through_the_entry_point_model(monkeypatch):
+    """Seeded random pairwise contractions -- up to three row, column and K indices, batch
+    indices, extents 1..5, sliced and permuted operand views, accumulation -- planned by
+    contract_f64 and executed by the numpy model of pcg_contract_f64, against numpy.einsum."""
+    import random
+    import string
+    import abi_model
+    from pycc_gb300.contract import contract_f64
+    abi_model.install(monkeypatch)
+    random.seed(1)
+    rng = np.random.default_rng(1)
+    ran = 0
+    while ran < 300:
+        letters = random.sample(string.ascii_lowercase, 8)
+        nm, nn, nk, nb = (random.randint(0, 3), random.randint(0, 3), random.randint(0, 3),
+                          random.choice([0, 0, 1]))
+        if nm + nk + nb > 4 or nn + nk + nb > 4 or nm + nn + nb + nk == 0:
+            continue
+        M, N = letters[:nm], letters[nm:nm + nn]
+        K, Bt = letters[nm + nn:nm + nn + nk], letters[nm + nn + nk:nm + nn + nk + nb]
+        ext = {c: random.randint(1, 5) for c in M + N + K + Bt}
+        la, lb, rhs = M + K + Bt, N + K + Bt, M + N + Bt
+        for lab in (la, lb, rhs):
+            random.shuffle(lab)
+
+        def view(labels):
+            base = torch.from_numpy(rng.standard_normal([ext[c] + random.randint(0, 2)
+                                                         for c in labels]))
+            return base[tuple(slice(0, ext[c]) for c in labels)]
+        A, B = view(la), view(lb)
+        out = torch.from_numpy(rng.standard_normal([ext[c] for c in rhs]))
+        subs = "%s,%s->%s" % ("".join(la), "".join(lb), "".join(rhs))
+        want = 0.5 * out.numpy() + 1.5 * np.einsum(subs, A.numpy(), B.numpy())
+        contract_f64(subs, A, B, out=out, alpha=1.5, beta=0.5)
+        assert np.allclose(out.numpy(), want, rtol=1e-12, atol=1e-12), subs
+        ran += 1

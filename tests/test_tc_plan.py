@@ -158,3 +158,62 @@ def test_swapped_integrals_drop_the_packs():
     w.h.ERI = t(5, 5, 5, 5)                             # a plain array is refused
     with pytest.raises(TypeError):
         m.sync_integrals()
+
+
+def test_random_contractions_through_the_entry_point_model(monkeypatch):
+    """Seeded random contractions on the tensor-core engine -- operand combinations
+    a X + b Y' (Y in another label order) and c P (x) Q, static and dynamic operands, every
+    GEMM format, sliced views, extents 1..6 -- packed and multiplied by the exact FP64 model
+    of pcg_pack_operand / pcg_tc_gemm, against numpy.einsum of the same combinations."""
+    import random
+    import string
+    import numpy as np
+    import abi_model
+    abi_model.install(monkeypatch)
+    random.seed(2)
+    rng = np.random.default_rng(2)
+    eng = TCEngine("cpu")
+    fmts = [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_BF16X6, FMT_FP8]
+    ran = 0
+    while ran < 200:
+        letters = random.sample(string.ascii_lowercase, 8)
+        nm, nn, nk = random.randint(0, 3), random.randint(0, 3), random.randint(1, 3)
+        if nm + nk > 4 or nn + nk > 4 or nm + nn == 0:
+            continue
+        M, N, K = letters[:nm], letters[nm:nm + nn], letters[nm + nn:nm + nn + nk]
+        ext = {c: random.randint(1, 6) for c in M + N + K}
+        la, lb, rhs = M + K, N + K, M + N
+        for lab in (la, lb, rhs):
+            random.shuffle(lab)
+
+        def view(labels):
+            base = torch.from_numpy(rng.standard_normal([ext[c] + random.randint(0, 2)
+                                                         for c in labels]))
+            return base[tuple(slice(0, ext[c]) for c in labels)]
+
+        def operand(labels, key):
+            s = "".join(labels)
+            X = view(labels)
+            op, val = Operand(s, (X, s), key=key), X.numpy().copy()
+            if len(labels) >= 2 and random.random() < 0.5:
+                perm = labels[:]
+                random.shuffle(perm)
+                Y = view(perm)
+                op.Y, op.b = (Y, "".join(perm)), -0.5
+                val = val - 0.5 * np.einsum("%s->%s" % ("".join(perm), s), Y.numpy())
+            if len(labels) >= 2 and random.random() < 0.5:
+                cut = random.randint(1, len(labels) - 1)
+                P, Q = view(labels[:cut]), view(labels[cut:])
+                op.P, op.Q, op.c = (P, "".join(labels[:cut])), (Q, "".join(labels[cut:])), 0.75
+                val = val + 0.75 * np.einsum("%s,%s->%s" % ("".join(labels[:cut]),
+                                                              "".join(labels[cut:]), s),
+                                             P.numpy(), Q.numpy())
+            return op, val
+        A, va = operand(la, None)
+        B, vb = operand(lb, ("static", ran) if random.random() < 0.5 else None)
+        out = torch.from_numpy(rng.standard_normal([ext[c] for c in rhs]))
+        subs = "%s,%s->%s" % ("".join(la), "".join(lb), "".join(rhs))
+        want = 0.25 * out.numpy() + 2.0 * np.einsum(subs, va, vb)
+        eng.contract(subs, A, B, out, alpha=2.0, beta=0.25, fmt=random.choice(fmts))
+        assert np.allclose(out.numpy(), want, rtol=1e-11, atol=1e-11), subs
+        ran += 1
