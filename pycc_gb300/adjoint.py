@@ -16,8 +16,15 @@ gives the vector-Jacobian products of the residual:
   The reference stores representative blocks and symmetrises them 4-fold; both agree on the
   8-fold permutationally symmetric projection, the part any symmetric perturbation sees.
 
-vvvv-sized cotangents are never stored separately: the ladder's adjoint contractions write
-straight into the gradient buffers of tau and of the <ab|ef> block.
+* J x (the forward sweep over the same tape, each op's tangent rule): the CCSD Jacobian
+  applied to an amplitude pair, the reference's ``CCderiv._ccsd_jacobian``
+  (``pycc/ccderiv.py:149-180``), exact because every taped op is linear or bilinear.
+
+The sweeps' contractions run on the FP64 DMMA kernel, or, with ``sweep='tc'``, the large
+GEMM-shaped ones on the tcgen05 engine in split-BF16x3.  vvvv-sized cotangents are never
+stored separately: the ladder's adjoint contractions write straight into the gradient
+buffers of tau and of the <ab|ef> block.  ``pycc_gb300.lagrangian`` wraps the sweeps in the
+reference's ``cchbar`` / ``cclambda`` / ``ccdensity`` objects.
 """
 from __future__ import annotations
 
