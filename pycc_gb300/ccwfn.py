@@ -19,6 +19,7 @@ There is no CPU fallback: ``device='CPU'`` is the reference's own code path.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 import time
 
@@ -32,6 +33,24 @@ from .exceptions import ConvergenceError, InvalidKeywordError, NumericalError, P
 from .hamiltonian import Hamiltonian
 
 WORK_LEN = 4096
+
+
+def _lagrange_at_i(nodes):
+    """Weights w_k with p(i) = sum_k w_k p(s_k) for every polynomial p of degree < len(nodes)."""
+    out = []
+    for k, sk in enumerate(nodes):
+        num, den = 1.0 + 0.0j, 1.0
+        for j, sj in enumerate(nodes):
+            if j != k:
+                num *= 1j - sj
+                den *= sk - sj
+        out.append(num / den)
+    return tuple(out)
+
+
+# nodes of the complex-residual evaluation and their weights at s = i
+_CNODES = (-2.0, -1.0, 0.0, 1.0, 2.0)
+_CWEIGHTS = _lagrange_at_i(_CNODES)
 
 
 def _ptr(t):
@@ -136,7 +155,6 @@ class CCwfn:
         for name, what in (('make_t3_density', "(T) densities"),
                            ('store_triples', "stored CC3 triples"),
                            ('field', "a finite field"),
-                           ('real_time', "real-time (complex) amplitudes"),
                            ('localize_occ', "localised occupied orbitals")):
             if kwargs.pop(name, False):
                 raise NotImplementedError("%s=True: %s are not part of the GPU engine"
@@ -154,7 +172,10 @@ class CCwfn:
         if local_mos not in ('PIPEK_MEZEY', 'BOYS'):
             raise InvalidKeywordError('local_mos', local_mos, ['PIPEK_MEZEY', 'BOYS'])
         self.local_mos = local_mos
-        self.make_t3_density = self.store_triples = self.field = self.real_time = False
+        self.make_t3_density = self.store_triples = self.field = False
+        # for CCSD the flag changes nothing (the reference's CC3 triples read it); complex
+        # amplitudes are recognised by their dtype
+        self.real_time = bool(kwargs.pop('real_time', False))
 
     # -- amplitude views ------------------------------------------------------------------
     @property
@@ -362,9 +383,14 @@ class CCwfn:
 
     # -- pycc/ccwfn.py:321-372 ------------------------------------------------------------
     def residuals(self, F, t1, t2, real_time=False):
-        """(r1, r2) for the current amplitudes; r2 symmetrised, FP64 on the GPU."""
-        if real_time:
-            raise NotImplementedError("real-time (complex) residuals are not part of the GPU engine")
+        """(r1, r2) for the current amplitudes; r2 symmetrised, FP64 on the GPU.
+
+        ``real_time`` is accepted as the reference accepts it: for CCSD it changes nothing
+        (only the reference's CC3 triples read it).  Complex F, t1 or t2 -- the amplitudes of
+        the reference's real-time propagation -- give complex residuals (``_complex_residuals``).
+        """
+        if any(torch.is_complex(x) for x in (F, t1, t2)):
+            return self._complex_residuals(F, t1, t2)
         if self.precision in ('MIXED', 'SP'):
             return self.mixed_engine().residuals(F, t1, t2)
         o, v = self.o, self.v
@@ -379,6 +405,50 @@ class CCwfn:
         r1 = self.r_T1(o, v, F, ERI, L, t1, t2, Fae, Fme, Fmi)
         r2 = self.r_T2(o, v, F, ERI, t1, t2, Fae, Fme, Fmi, Wmnij, Wmbej, Wmbje, Zmbij)
         return r1, r2
+
+    def _complex_residuals(self, F, t1, t2):
+        """Residuals at complex (F, t1, t2) from five real ones.  Along
+        s -> (F_r + s F_i, t_r + s t_i) the residual is a polynomial of degree <= 4 in s
+        (terms are at most quartic in t and at most linear in F, and F never multiplies a
+        quartic), so its value at s = i is the Lagrange interpolant through s = -2 .. 2,
+        evaluated at i: r(F, t) = sum_k w_k r(F_r + s_k F_i, t_r + s_k t_i), exactly.
+        The weights are at most 2.5 in modulus, so rounding is not amplified."""
+        def parts(x):
+            if torch.is_complex(x):
+                return x.real.contiguous(), x.imag.contiguous()
+            return x.contiguous(), torch.zeros_like(x)
+        (Fr, Fi), (ar, ai), (br, bi) = parts(F), parts(t1), parts(t2)
+        r1s, r2s = [], []
+        for s in _CNODES:
+            pts = []
+            for re, im in ((Fr, Fi), (ar, ai), (br, bi)):
+                pts.append(self._axpy(re, s, im))
+            r1, r2 = self.residuals(*pts)
+            r1s.append(r1)
+            r2s.append(r2)
+        out = []
+        for rs in (r1s, r2s):
+            re = self._lincomb(rs, [w.real for w in _CWEIGHTS])
+            im = self._lincomb(rs, [w.imag for w in _CWEIGHTS])
+            out.append(torch.complex(re, im))
+        return out[0], out[1]
+
+    def _axpy(self, x, s, y):
+        """x + s y into a fresh contiguous FP64 tensor (FP64 kernel)."""
+        out = torch.empty(x.shape, dtype=torch.float64, device=x.device)
+        ptrs = (C.c_void_p * 2)(x.data_ptr(), y.data_ptr())
+        coef = (C.c_double * 2)(1.0, float(s))
+        _lib.call("pcg_lincomb_f64", ptrs, coef, 2, x.numel(), out.data_ptr(), self._st())
+        return out
+
+    def _lincomb(self, xs, cs):
+        """sum_k cs[k] xs[k] into a fresh tensor (FP64 kernel; the xs are contiguous)."""
+        xs = [x.contiguous() for x in xs]
+        out = torch.empty_like(xs[0])
+        ptrs = (C.c_void_p * len(xs))(*[x.data_ptr() for x in xs])
+        coef = (C.c_double * len(xs))(*[float(c) for c in cs])
+        _lib.call("pcg_lincomb_f64", ptrs, coef, len(xs), out.numel(), out.data_ptr(), self._st())
+        return out
 
     def mixed_engine(self):
         if self._mixed is None:

@@ -8,11 +8,11 @@ with ``CCwfn.__new__`` plus the attributes that ``CCwfn.__init__`` would have se
 (``pycc/ccwfn.py:76-213``, ``pycc/wavefunction.py:293-332``), on the synthetic
 Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
 ``residuals`` / ``solve_cc`` / ``t_vikings`` / ``t_tjl`` / ``cchbar`` -> ``cclambda``
--> ``ccdensity`` / ``CCderiv._ccsd_jacobian`` and stores their outputs as ``.npz`` fixtures next to this file.
+-> ``ccdensity`` / ``CCderiv._ccsd_jacobian`` and the complex residual, and stores their outputs as ``.npz`` fixtures next to this file.
 
 Usage::
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian]
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian] [--no-complex]
 
 The no=20, nv=180 fixtures need ~30 GB of host RAM and several minutes.
 """
@@ -206,6 +206,26 @@ def gen_o5v19_jacobian(pycc):
           % (np.linalg.norm(out["sigma1"]), np.linalg.norm(out["sigma2_sym"])))
 
 
+def gen_o5v19_complex(pycc):
+    """The reference's residual at complex amplitudes and a complex Fock matrix, as its
+    real-time propagation calls it (``residuals(F, t1, t2, real_time=True)``): no=5, nv=19,
+    seeded complex t1 / t2 (t2_ijab = t2_jiba) and F + i dF with a real symmetric dF."""
+    no, nv, seed = WORKLOADS["o5v19"]
+    fac = SyntheticFactors(no, nv, seed)
+    F, ERI, L = fac.hamiltonian()
+    w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
+    rng = np.random.default_rng(3000 + seed)
+    t1 = 0.05 * (rng.standard_normal((no, nv)) + 1j * rng.standard_normal((no, nv)))
+    t2 = 0.05 * (rng.standard_normal((no, no, nv, nv)) + 1j * rng.standard_normal((no, no, nv, nv)))
+    t2 = t2 + t2.transpose(1, 0, 3, 2)
+    dF = rng.standard_normal(F.shape)
+    Fc = F + 0.01j * (dF + dF.T)
+    r1, r2 = w.residuals(Fc, t1, t2, real_time=True)
+    np.savez_compressed(os.path.join(HERE, "o5v19_complex.npz"), F=Fc, t1=t1, t2=t2,
+                        r1=np.asarray(r1), r2=np.asarray(r2))
+    print("o5v19_complex: |r1| = %.6e  |r2| = %.6e" % (np.linalg.norm(r1), np.linalg.norm(r2)))
+
+
 def gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz"):
     """no=20, nv=180, seed 1.  With the spec's plain sigma (coupling 1) CCSD diverges at this
     size, so the converged fixture uses the matched coupling; the raw-sigma fixture keeps the
@@ -256,12 +276,15 @@ def main():
     ap.add_argument("--o20v180", action="store_true")
     ap.add_argument("--no-o5v19", action="store_true")
     ap.add_argument("--no-jacobian", action="store_true")
+    ap.add_argument("--no-complex", action="store_true")
     args = ap.parse_args()
     pycc = import_reference()
     if not args.no_o5v19:
         gen_o5v19(pycc)
     if not args.no_jacobian:
         gen_o5v19_jacobian(pycc)
+    if not args.no_complex:
+        gen_o5v19_complex(pycc)
     if args.o20v180:
         gen_o20v180(pycc, solve=False, coupling=1.0, name="o20v180_raw.npz")
         gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz")
