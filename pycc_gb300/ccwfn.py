@@ -57,6 +57,13 @@ def _ptr(t):
     return t.data_ptr()
 
 
+def _f64(what, *ts):
+    """The FP64 kernels read raw pointers: refuse any other dtype instead of misreading it."""
+    for t in ts:
+        if t.dtype != torch.float64:
+            raise TypeError("%s: float64 tensors expected, got %s" % (what, t.dtype))
+
+
 class CCwfn:
     """RHF-CCSD wave function on one GPU (mirrors ``pycc/ccwfn.py:32-213``).
 
@@ -243,7 +250,12 @@ class CCwfn:
 
     # -- pycc/ccwfn.py:432-455 ------------------------------------------------------------
     def build_tau(self, t1, t2, fact1=1.0, fact2=1.0):
-        """tau_ijab = fact1 t2_ijab + fact2 t_ia t_jb (fused FP64 kernel)."""
+        """tau_ijab = fact1 t2_ijab + fact2 t_ia t_jb (fused FP64 kernel; complex amplitudes
+        through five real evaluations, ``_complex_eval``)."""
+        if torch.is_complex(t1) or torch.is_complex(t2):
+            return self._complex_eval(lambda a, b: (self.build_tau(a, b, fact1, fact2),),
+                                      t1, t2)[0]
+        _f64("build_tau", t1, t2)
         if not (t1.is_contiguous() and t2.is_contiguous()):
             raise ValueError("build_tau: t1 and t2 must be contiguous")
         out = torch.empty_like(t2)
@@ -255,6 +267,7 @@ class CCwfn:
 
     def _combine(self, a, X, b, Y, perm_y, out=None, record=True):
         """out_pqrs = a X_pqrs + b Y_perm (4-index; perm_y permutes Y's axes)."""
+        _f64("_combine", X, *([Y] if Y is not None else []), *([out] if out is not None else []))
         fresh = out is None
         ext = list(X.shape)
         if out is None:
@@ -407,31 +420,30 @@ class CCwfn:
         return r1, r2
 
     def _complex_residuals(self, F, t1, t2):
-        """Residuals at complex (F, t1, t2) from five real ones.  Along
+        """Residuals at complex (F, t1, t2) from five real ones (``_complex_eval``): along
         s -> (F_r + s F_i, t_r + s t_i) the residual is a polynomial of degree <= 4 in s
         (terms are at most quartic in t and at most linear in F, and F never multiplies a
-        quartic), so its value at s = i is the Lagrange interpolant through s = -2 .. 2,
-        evaluated at i: r(F, t) = sum_k w_k r(F_r + s_k F_i, t_r + s_k t_i), exactly.
-        The weights are at most 2.5 in modulus, so rounding is not amplified."""
+        quartic)."""
+        return self._complex_eval(lambda *a: self.residuals(*a), F, t1, t2)
+
+    def _complex_eval(self, fn, *args):
+        """fn at complex arguments, for an fn whose value along s -> (re + s im) is a
+        polynomial of degree <= 4 in s: the Lagrange interpolant through s = -2 .. 2,
+        evaluated at s = i, sum_k w_k fn(re + s_k im), exactly.  The weights are at most 2.5
+        in modulus, so rounding is not amplified.  fn returns a tuple of real tensors."""
         def parts(x):
             if torch.is_complex(x):
                 return x.real.contiguous(), x.imag.contiguous()
             return x.contiguous(), torch.zeros_like(x)
-        (Fr, Fi), (ar, ai), (br, bi) = parts(F), parts(t1), parts(t2)
-        r1s, r2s = [], []
-        for s in _CNODES:
-            pts = []
-            for re, im in ((Fr, Fi), (ar, ai), (br, bi)):
-                pts.append(self._axpy(re, s, im))
-            r1, r2 = self.residuals(*pts)
-            r1s.append(r1)
-            r2s.append(r2)
+        split = [parts(x) for x in args]
+        vals = [fn(*[self._axpy(re, s, im) for re, im in split]) for s in _CNODES]
         out = []
-        for rs in (r1s, r2s):
-            re = self._lincomb(rs, [w.real for w in _CWEIGHTS])
-            im = self._lincomb(rs, [w.imag for w in _CWEIGHTS])
+        for q in range(len(vals[0])):
+            xs = [v[q] for v in vals]
+            re = self._lincomb(xs, [w.real for w in _CWEIGHTS])
+            im = self._lincomb(xs, [w.imag for w in _CWEIGHTS])
             out.append(torch.complex(re, im))
-        return out[0], out[1]
+        return tuple(out)
 
     def _axpy(self, x, s, y):
         """x + s y into a fresh contiguous FP64 tensor (FP64 kernel)."""
@@ -464,7 +476,13 @@ class CCwfn:
         return E
 
     def cc_energy(self, o, v, F, L, t1, t2, out=None):
-        """E = 2 f_ia t_ia + tau_ijab L_ijab as a 0-d FP64 GPU tensor (fused kernel)."""
+        """E = 2 f_ia t_ia + tau_ijab L_ijab as a 0-d FP64 GPU tensor (fused kernel).  Complex
+        F / t1 / t2 (the reference's real-time propagation) give a complex 0-d tensor, through
+        five real evaluations (``_complex_eval``)."""
+        if any(torch.is_complex(x) for x in (F, t1, t2)):
+            return self._complex_eval(lambda f, a, b: (self.cc_energy(o, v, f, L, a, b),),
+                                      F, t1, t2)[0]
+        _f64("cc_energy", F, t1, t2)
         t1 = t1.contiguous()
         t2 = t2.contiguous()
         Fov = F[o, v]
@@ -486,6 +504,7 @@ class CCwfn:
             _lib.call("pcg_inv_denominators_f64", _ptr(self.H.eps), no, nv, _ptr(self._inv),
                       _ptr(self._inv[n1:]), self._st())
         out = self._scalars[1:3]
+        _f64("update_amplitudes", r1, r2)
         r1 = r1.contiguous()
         r2 = r2.contiguous()
         _lib.call("pcg_update_inv_f64", _ptr(self.t1), _ptr(r1), _ptr(self._inv), n1,

@@ -55,3 +55,28 @@ def test_real_inputs_unchanged_by_the_flag(model, ham_o5v19, golden_o5v19):
     assert (c1.real - r1).abs().max().item() < 1e-14 * r1.abs().max().item()
     assert c1.imag.abs().max().item() < 1e-14 * r1.abs().max().item()
     assert (c2.real - r2).abs().max().item() < 1e-14 * r2.abs().max().item()
+
+
+def test_complex_energy_and_tau(model, ham_o5v19):
+    """cc_energy and build_tau at complex amplitudes (the real-time propagation's energy)
+    against the oracle's formulas evaluated in complex arithmetic; other dtypes are refused
+    rather than misread by the FP64 kernels."""
+    from oracle import ccsd as oc
+    g = golden("o5v19_complex.npz")
+    _, F, ERI, L = ham_o5v19
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu"))
+    Fc, t1, t2 = (torch.from_numpy(g[k]) for k in ("F", "t1", "t2"))
+    o, v = w.o, w.v
+    e = w.cc_energy(o, v, Fc, w.H.L, t1, t2)
+    # E = 2 f_ia t_ia + (t2_ijab + t_ia t_jb) L_ijab (pycc/ccwfn.py:1122-1162), in complex
+    # arithmetic (the oracle's cc_energy returns a real float)
+    tau_c = g["t2"] + np.einsum("ia,jb->ijab", g["t1"], g["t1"])
+    want = 2.0 * np.sum(g["F"][o, v] * g["t1"]) + np.sum(tau_c * L[o, o, v, v])
+    assert e.dtype == torch.complex128 and abs(complex(e) - want) < 1e-13 * abs(want)
+    tau = w.build_tau(t1, t2, 1.0, 0.5)
+    want_tau = oc.build_tau(g["t1"], g["t2"], 1.0, 0.5)
+    assert np.abs(tau.numpy() - want_tau).max() < 1e-14 * np.abs(want_tau).max()
+    with pytest.raises(TypeError):
+        w.build_tau(t1.real.float().contiguous(), t2.real.float().contiguous())
+    with pytest.raises(TypeError):
+        w.cc_energy(o, v, w.H.F, w.H.L, t1.real.float().contiguous(), t2.real.contiguous())
