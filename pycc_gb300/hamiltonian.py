@@ -63,9 +63,15 @@ def _sl(pat, no, nv):
 
 
 def _host(x):
-    """A float64 numpy view or copy of a numpy array or torch tensor (any device)."""
+    """A float64 numpy view or copy of a numpy array or torch tensor (any device).  Complex
+    input is refused: the resident blocks are real, and a complex Fock matrix (a real-time
+    field) is passed to ``CCwfn.residuals`` / ``cc_energy`` directly."""
     if isinstance(x, torch.Tensor):
+        if torch.is_complex(x):
+            raise TypeError("Hamiltonian: complex integrals are not supported")
         x = x.detach().to("cpu", torch.float64).numpy()
+    if np.iscomplexobj(x):
+        raise TypeError("Hamiltonian: complex integrals are not supported")
     return np.asarray(x, dtype=np.float64)
 
 

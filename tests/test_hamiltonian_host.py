@@ -43,3 +43,11 @@ def test_block_indexing_errors(ham_o5v19):
         H.ERI[slice(0, 3), v, v, v]                     # not the occupied space
     with pytest.raises(KeyError, match="not resident"):
         H.L[v, v, v, v]                                 # L keeps only the residual's blocks
+
+
+def test_complex_input_refused(ham_o5v19):
+    _, F, ERI, _ = ham_o5v19
+    with pytest.raises(TypeError):
+        Hamiltonian.from_arrays(F + 0.01j, ERI, 5, device="cpu")
+    with pytest.raises(TypeError):
+        Hamiltonian.from_arrays(torch.from_numpy(F).to(torch.complex128), ERI, 5, device="cpu")
