@@ -151,3 +151,28 @@ def test_max_diis_zero_keeps_no_history(fake):
 def test_negative_max_diis_rejected():
     with pytest.raises(ValueError):
         DIIS(torch.zeros(4, dtype=torch.float64), -1)
+
+
+@pytest.mark.parametrize("max_diis,start", [(8, 1), (3, 2), (0, 1)])
+def test_helper_diis_interface(fake, max_diis, start):
+    """pycc_gb300.utils.helper_diis keeps the reference's interface -- separate t1 / t2,
+    add_error_vector(t1, t2), extrapolate(t1, t2) -> (t1, t2) -- and its results."""
+    from pycc_gb300.utils import helper_diis
+    t1s, t2s = _sequence(6, 50, 12, max_diis + 10 * start)
+    sh1, sh2 = (3, 2), (5, 10)
+    d = helper_diis(torch.from_numpy(t1s[0].reshape(sh1)), torch.from_numpy(t2s[0].reshape(sh2)),
+                    max_diis)
+    ref = oc.DIIS(t1s[0], t2s[0], max_diis)
+    for n, (a, b) in enumerate(zip(t1s[1:], t2s[1:]), start=1):
+        ta, tb = torch.from_numpy(a.reshape(sh1)), torch.from_numpy(b.reshape(sh2))
+        d.add_error_vector(ta, tb)
+        ref.add_error_vector(a, b)
+        if n >= start:
+            ga, gb = d.extrapolate(ta, tb)
+            wa, wb = ref.extrapolate(a, b)
+            assert tuple(ga.shape) == sh1 and tuple(gb.shape) == sh2
+            scale = max(np.abs(wa).max(), np.abs(wb).max())
+            assert np.abs(ga.numpy().ravel() - wa).max() <= 1e-12 * scale
+            assert np.abs(gb.numpy().ravel() - wb).max() <= 1e-12 * scale
+    with pytest.raises(TypeError):
+        helper_diis(torch.zeros(2, dtype=torch.float32), torch.zeros(3), 8)
