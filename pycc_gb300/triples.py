@@ -130,3 +130,16 @@ def t_energy(w, t1=None, t2=None):
         return t_energy_fp64(w, t1, t2)
     from .triples_tc import t_energy_tc
     return t_energy_tc(w, t1, t2)
+
+
+def t_tjl(ccwfn):
+    """The reference's entry point ``t_tjl(ccwfn) -> float`` (``pycc/cctriples.py:177-240``):
+    E(T) at ``ccwfn``'s amplitudes, in its precision (``t_energy``)."""
+    return t_energy(ccwfn)
+
+
+def t_vikings(ccwfn):
+    """``t_vikings(ccwfn) -> float`` (``pycc/cctriples.py:243-308``): the reference's
+    full-(i,j,k) formulation of the same E(T); the engine evaluates it over i >= j >= k with
+    the Lee-Rendell weights, which gives the same value (``t_energy``)."""
+    return t_energy(ccwfn)

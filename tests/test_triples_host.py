@@ -77,3 +77,10 @@ def test_degenerate_sizes(model, no, nv):
     assert abs(t_energy_fp64(w) - ref) < 1e-13 * max(1.0, abs(ref))
     for batch in (1, 32):
         assert abs(t_energy_tc(w, batch=batch) - ref) < 1e-6 * max(abs(ref), 1e-8)
+
+
+def test_reference_entry_point_names(model, ham_o5v19, golden_o5v19):
+    from pycc_gb300.triples import t_tjl, t_vikings
+    w = converged(ham_o5v19, golden_o5v19)
+    assert abs(t_tjl(w) - float(golden_o5v19["et_tjl"])) < 1e-13
+    assert abs(t_vikings(w) - float(golden_o5v19["et_vikings"])) < 1e-13
