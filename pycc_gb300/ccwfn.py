@@ -447,6 +447,7 @@ class CCwfn:
 
     def _axpy(self, x, s, y):
         """x + s y into a fresh contiguous FP64 tensor (FP64 kernel)."""
+        _f64("complex evaluation (complex128 / float64 inputs)", x, y)
         out = torch.empty(x.shape, dtype=torch.float64, device=x.device)
         ptrs = (C.c_void_p * 2)(x.data_ptr(), y.data_ptr())
         coef = (C.c_double * 2)(1.0, float(s))

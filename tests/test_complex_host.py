@@ -80,3 +80,15 @@ def test_complex_energy_and_tau(model, ham_o5v19):
         w.build_tau(t1.real.float().contiguous(), t2.real.float().contiguous())
     with pytest.raises(TypeError):
         w.cc_energy(o, v, w.H.F, w.H.L, t1.real.float().contiguous(), t2.real.contiguous())
+
+
+def test_single_precision_complex_refused(model, ham_o5v19):
+    """complex64 (or float32 next to complex) inputs are refused, not misread as FP64."""
+    g = golden("o5v19_complex.npz")
+    _, F, ERI, L = ham_o5v19
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu"))
+    Fc, t1, t2 = (torch.from_numpy(g[k]) for k in ("F", "t1", "t2"))
+    with pytest.raises(TypeError):
+        w.residuals(Fc, t1.to(torch.complex64), t2)
+    with pytest.raises(TypeError):
+        w.residuals(Fc.real.float(), t1, t2)
