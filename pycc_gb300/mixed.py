@@ -58,6 +58,7 @@ class MixedResidual:
         self.history = []
         self.profile = None       # list of (subscripts, fmt, start, end) events when set
         self._pairs = None        # i <= j pair tables of the ladder
+        self._hole_tab = None     # the pair columns of Wmnij for the hole ladder
         self._r_seed = None
         self._blocks = None       # the integral blocks the caches were built from
 
@@ -196,6 +197,28 @@ class MixedResidual:
                          col_map=cmap, col_scale=csc)
         torch.cuda.nvtx.range_pop()
 
+    def hole_ladder_pairs(self, t1, t2, Wmnij, r):
+        """r_ijab += 1/2 tau_mnab W_mnij (pycc/ccwfn.py:930) through the i <= j pairs only.
+
+        W_nmji = W_mnij and tau_nmba = tau_mnab, so the term is symmetric under
+        (i<->j, a<->b), as the particle ladder is: the same output map and 1/2 diagonal weights
+        (``ladder_pairs``) apply, with a row table selecting the pair columns of W_mnij.
+        """
+        no = self.w.no
+        if self._hole_tab is None:
+            ii, jj = np.triu_indices(no)
+            tab = np.zeros((4, ii.size), dtype=np.int64)
+            tab[0] = ii * no + jj                        # Wmnij[m, n, i, j]
+            self._hole_tab = torch.from_numpy(tab).to(self.w.device1)
+        _, cmap, csc = self._pair_tables()
+        fmt = self.fmt()
+        tau = Operand('mnab', (t2, 'mnab'), P=(t1, 'ma'), Q=(t1, 'nb'), c=1.0)
+        pa = self.tc._pack(tau, ['a', 'b'], ['m', 'n'], fmt, 'A')
+        pb = pack(Operand.of('mnij', Wmnij), ['i', 'j'], ['m', 'n'], fmt, self.w.stream,
+                  row_tab=self._hole_tab)
+        self.tc.run_gemm('mnab,mnij->ijab', fmt, pa, pb, r, ['a', 'b'], [], 'ijab', 1.0, 1.0,
+                         col_map=cmap, col_scale=csc)
+
     # -- intermediates (pycc/ccwfn.py:458-715) -------------------------------------------
     def build_Fae(self, F, t1, t2):
         o, v = self.w.o, self.w.v
@@ -290,18 +313,18 @@ class MixedResidual:
         contract_f64('je,me->mj', t1, Fme, out=Fmj, alpha=0.5, beta=1.0)
         self.tcc('imab,mj->ijab', Operand.of('imab', t2), Operand.of('mj', Fmj), r, alpha=-1.0)
         # ladders
-        tau_mn = Operand('mnab', (t2, 'mnab'), P=(t1, 'ma'), Q=(t1, 'nb'), c=1.0)
-        self.tcc('mnab,mnij->ijab', tau_mn, Operand.of('mnij', Wmnij), r, alpha=0.5)
+        self.hole_ladder_pairs(t1, t2, Wmnij, r)
         self.ladder_pairs(t1, t2, r, self.ladder_fmt())
         # - t_ma (Z_mbij + <mb|ij>) - t_ie t_ma <mb|ej> - t_ie t_mb <ma|je>, the last written
         # as its (i<->j, a<->b) image - t_je t_ma <mb|ie>, which the symmetrisation
         # r2 = h + h' sums to the same residual; the o^3 v tensors are summed in Zmbij
         self.tcc('ma,mbij->ijab', Operand.of('ma', t1), Operand.of('mbij', Zmbij), r, alpha=-1.0)
         # rings
-        self.tcc('imae,mbej->ijab', Operand('imae', (t2, 'imae'), Y=(t2, 'imea'), b=-1.0),
+        # (t2 - t2~) W + t2 (W + W~) regrouped as (2 t2 - t2~) W + t2 W~: the first operand
+        # is r_T1's, already packed this residual, and W~ is one source instead of two
+        self.tcc('imae,mbej->ijab', Operand('imae', (t2, 'imae'), a=2.0, Y=(t2, 'imea'), b=-1.0),
                  Operand.of('mbej', Wmbej), r)
-        self.tcc('imae,mbej->ijab', Operand.of('imae', t2),
-                 Operand('mbej', (Wmbej, 'mbej'), Y=(Wmbje, 'mbje'), b=1.0), r)
+        self.tcc('imae,mbej->ijab', Operand.of('imae', t2), Operand('mbej', (Wmbje, 'mbje')), r)
         self.tcc('mjae,mbie->ijab', Operand.of('mjae', t2), Operand.of('mbie', Wmbje), r)
         self.tcc('ie,abej->ijab', Operand.of('ie', t1), self.eri('vvvo', 'abej'), r)
         return r
