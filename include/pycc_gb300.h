@@ -162,21 +162,27 @@ int pcg_reduce_sum_f64(const double* x, long long n, double* out, void* stream);
  * 458-945 through pycc/device.py:64-87); the reference's own low-precision mode is plain
  * float32 (pycc/device.py:143-154).
  *
- * pcg_pack_operand: dst[r][k] = convert(a*X + b*Y + c*P*Q), each source read at
- *   rowoff_s(r) + koff_s(k); r (k) is a flat index over r_n (k_n) sub-indices with extents
- *   r_ext[q] and strides r_str[s*4 + q] for source s in (X, Y, P, Q) (0 = broadcast).
+ * pcg_pack_operand: dst[r][k] = convert(w_k * (a*X + b*Y + c*P*Q + d*R*S)), each source
+ *   read at rowoff_s(r) + koff_s(k); r (k) is a flat index over r_n (k_n) sub-indices with
+ *   extents r_ext[q] and strides r_str[s*4 + q] for source s in (X, Y, P, Q, R, S)
+ *   (0 = broadcast; 6 x 4 strides).
  *   Formats: 0 BF16 into hi; 1 BF16 hi + lo = bf16(v - hi); 2 FP8 E4M3 bytes into hi with
  *   row_scale[r] = 2^ceil(log2(max_k |v| / 448)); 3 three BF16 pieces hi = bf16(v),
  *   mid = bf16(v - hi), lo = bf16(v - hi - mid).  Rows are Kp elements long (zero padded);
- *   Kp is a multiple of 64 (BF16) or 128 (FP8).  X or P (with Q) must be given; Y may be
- *   NULL; mid is used by format 3 only.  row_tab (optional, device, [4][rows]) gives the
- *   four sources' row offsets explicitly (e.g. the i <= j pairs of a symmetric operand);
- *   the r sub-indices are then ignored and `rows` rows are packed. */
+ *   Kp is a multiple of 64 (BF16) or 128 (FP8).  X, P (with Q) or R (with S) must be
+ *   given; Y may be NULL; mid is used by format 3 only.  row_tab (optional, device,
+ *   [6][rows]) gives the six sources' row offsets explicitly (e.g. the i <= j pairs of a
+ *   symmetric operand); the r sub-indices then only tell the kernel which side is
+ *   unit-stride, and `rows` rows are packed.  k_tab (optional, device, [6][kcount]) does the
+ *   same for K (e.g. the e <= f pairs), with kcount K entries; k_w (optional, device,
+ *   kcount floats, needs k_tab) multiplies each K entry (w_k = 1 without it). */
 int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* r_str, int k_n,
                      const long long* k_ext, const long long* k_str, long long Kp, double a,
                      const double* X, double b, const double* Y, double c, const double* P,
-                     const double* Q, void* hi, void* mid, void* lo, float* row_scale,
-                     const long long* row_tab, long long rows, void* stream);
+                     const double* Q, double d, const double* R, const double* S, void* hi,
+                     void* mid, void* lo, float* row_scale, const long long* row_tab,
+                     long long rows, const long long* k_tab, const float* k_w,
+                     long long kcount, void* stream);
 
 /* pcg_tc_gemm: C[off_m(m) + off_n(n)] = beta*C + alpha * sum_k A[m][k] B[n][k] (C FP64).
  *   A: M rows of lda elements (K-major, 16-byte aligned rows), B: N rows of ldb elements;
@@ -198,6 +204,20 @@ int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, 
                 const long long* m_ext, const long long* m_sc, int n_n, const long long* n_ext,
                 const long long* n_sc, const long long* col_map, const double* col_scale,
                 double alpha, double beta, double* C, int* status, void* stream);
+
+/* pcg_ladder_pm_assemble: the particle-particle ladder 1/2 tau_ijef <ab|ef> (pycc/ccwfn.py:931,
+ *   the 'ijef,abef->ijab' contraction of ContractionBackend.__call__, pycc/device.py:64-87) in
+ *   symmetric / antisymmetric pair form, added into the half residual h of r_T2.  Gp:
+ *   [no(no+1)/2][nv(nv+1)/2] = 1/2 sum_{e<=f} T+_ij,ef V+_ab,ef over the i <= j and a <= b
+ *   pairs (row-major), Gm: [no(no-1)/2][nv(nv-1)/2] = 1/2 sum_{e<f} T-_ij,ef V-_ab,ef over the
+ *   i < j and a < b pairs, with T+- = tau_ijef +- tau_ijfe and V+- = <ab|ef> +- <ab|fe>
+ *   (V+_ab,ee = <ab|ee>), so Gp + sign(b - a) Gm = sum_ef tau_ijef <ab|ef>.  For i < j,
+ *   a <= b: h_ijab += Gp + Gm and, for a < b, h_jiab += Gp - Gm (the a > b element of pair
+ *   (i, j); h only enters through the symmetrisation r2 = h_ijab + h_jiba, so pair i < j
+ *   carries the whole term); for i = j: h_iiab += Gp (a < b) or Gp / 2 (a = b).
+ *   Gm may be NULL when it is empty (no = 1 or nv = 1). */
+int pcg_ladder_pm_assemble(const double* Gp, const double* Gm, long long no, long long nv,
+                           double* h, void* stream);
 
 /* Grouped segmented BF16 GEMM with FP32 output, the connected-triples builder of the (T)
  * correction (t3c_ijk, pycc/cctriples.py:56-67, for a batch of triples).  Group g computes

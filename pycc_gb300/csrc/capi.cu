@@ -19,7 +19,7 @@ void set_error(const char* fmt, ...) {
 
 extern "C" const char* pcg_last_error(void) { return pcg::g_err; }
 
-extern "C" int pcg_abi_version(void) { return 1; }
+extern "C" int pcg_abi_version(void) { return 2; }
 
 // Kernels launched by this library since it was loaded (all threads, all streams).
 extern "C" long long pcg_launch_count(void) { return pcg::g_launches.load(); }

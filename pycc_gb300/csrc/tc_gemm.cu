@@ -446,61 +446,69 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 }
 
 // ---------------------------------------------------------------------------------------
-// Pack: dst[r][k] = convert(a*X + b*Y + c*P*Q) at per-source offsets rowoff_s(r)+koff_s(k).
+// Pack: dst[r][k] = w(k) * convert(a*X + b*Y + c*P*Q + d*R*S) at per-source offsets
+// rowoff_s(r) + koff_s(k).
 // ---------------------------------------------------------------------------------------
+constexpr int kPackSrc = 6;  // sources X, Y, P, Q, R, S
 struct PackIdx {
   int n;
   long long ext[kMaxSub];
-  long long s[4][kMaxSub];  // strides of sources X, Y, P, Q
+  long long s[kPackSrc][kMaxSub];  // strides of each source
 };
 
-// Offsets of flat row (or K) index r in the four sources; r and the extents are below 2^31
+// Offsets of flat row (or K) index r in the six sources; r and the extents are below 2^31
 // (checked by the host), so the decomposition is 32-bit integer arithmetic.
-__device__ __forceinline__ void pack_offsets(const PackIdx& d, long long r, long long (&o)[4]) {
-  o[0] = o[1] = o[2] = o[3] = 0;
+__device__ __forceinline__ void pack_offsets(const PackIdx& d, long long r,
+                                             long long (&o)[kPackSrc]) {
+#pragma unroll
+  for (int s = 0; s < kPackSrc; ++s) o[s] = 0;
   unsigned rr = (unsigned)r;
   for (int q = d.n - 1; q >= 0; --q) {
     const unsigned e = (unsigned)d.ext[q];
     const long long x = rr % e;
     rr /= e;
-    o[0] += x * d.s[0][q];
-    o[1] += x * d.s[1][q];
-    o[2] += x * d.s[2][q];
-    o[3] += x * d.s[3][q];
+#pragma unroll
+    for (int s = 0; s < kPackSrc; ++s) o[s] += x * d.s[s][q];
   }
 }
 
 struct PackArgs {
   PackIdx r, k;
   long long R, K, Kp;
-  double a, b, c;
+  double a, b, c, d;
   const double* X;
   const double* Y;
   const double* P;
   const double* Q;
+  const double* R2;
+  const double* S2;
   void* hi;
   void* lo;
   void* mid;
   float* scale;
-  const long long* row_tab;  // optional [4][R] per-source row offsets (replaces r)
+  const long long* row_tab;  // optional [6][R] per-source row offsets (replaces r)
+  const long long* k_tab;    // optional [6][K] per-source K offsets (replaces k)
+  const float* k_w;          // optional [K] multipliers of the K entries
   int fmt;
 };
 
 // Tiled pack: a block handles TR rows x TK columns of K.  Row and column offsets of the
-// four sources are decomposed once per tile into shared memory; values are gathered along
-// whichever index is unit-stride in X (kfast) and written out along K, so both the FP64
-// reads and the packed writes are coalesced.  The value type V is double for BF16x6 (three
-// pieces carry 24 bits) and float otherwise: FP64 inputs are rounded to FP32 in integer
-// arithmetic (f64_to_f32) and combined and split in FP32, which keeps the kernel a stream
-// instead of a loop on GB300's FP64 pipe.  A BF16 hi/lo pair holds 16 bits, so the FP32
-// rounding (2^-24 of the operands) is far below the split's own error.
+// six sources are decomposed (or read from the tables) once per tile into shared memory;
+// values are gathered along whichever index is unit-stride in X (kfast) and written out
+// along K, so both the FP64 reads and the packed writes are coalesced.  The value type V is
+// double for BF16x6 (three pieces carry 24 bits) and float otherwise: FP64 inputs are
+// rounded to FP32 in integer arithmetic (f64_to_f32) and combined and split in FP32, which
+// keeps the kernel a stream instead of a loop on GB300's FP64 pipe.  A BF16 hi/lo pair
+// holds 16 bits, so the FP32 rounding (2^-24 of the operands) is far below the split's own
+// error.  The K multipliers are powers of two in practice (exact in FP32).
 constexpr int TR = 64, TK = 64, PACK_THREADS = 256;
 static_assert((TR * TK) % PACK_THREADS == 0, "pack tile: whole elements per thread");
 
 template <typename V>
 struct PackTile {
-  long long rof[4][TR];
-  long long kof[4][TK];
+  long long rof[kPackSrc][TR];
+  long long kof[kPackSrc][TK];
+  V kw[TK];
   V v[TR][TK + 1];
 };
 
@@ -515,22 +523,30 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
                                                long long k0) {
   const int tid = threadIdx.x;
   if (tid < TR) {
-    long long o[4] = {0, 0, 0, 0};
+    long long o[kPackSrc] = {0, 0, 0, 0, 0, 0};
     if (r0 + tid < p.R) {
       if (p.row_tab)
-        for (int s = 0; s < 4; ++s) o[s] = p.row_tab[s * p.R + r0 + tid];
+        for (int s = 0; s < kPackSrc; ++s) o[s] = p.row_tab[s * p.R + r0 + tid];
       else
         pack_offsets(p.r, r0 + tid, o);
     }
-    for (int s = 0; s < 4; ++s) t.rof[s][tid] = o[s];
+    for (int s = 0; s < kPackSrc; ++s) t.rof[s][tid] = o[s];
   } else if (tid >= TR && tid < TR + TK) {
     const int j = tid - TR;
-    long long o[4] = {0, 0, 0, 0};
-    if (k0 + j < p.K) pack_offsets(p.k, k0 + j, o);
-    for (int s = 0; s < 4; ++s) t.kof[s][j] = o[s];
+    long long o[kPackSrc] = {0, 0, 0, 0, 0, 0};
+    V w = (V)1;
+    if (k0 + j < p.K) {
+      if (p.k_tab)
+        for (int s = 0; s < kPackSrc; ++s) o[s] = p.k_tab[s * p.K + k0 + j];
+      else
+        pack_offsets(p.k, k0 + j, o);
+      if (p.k_w) w = (V)p.k_w[k0 + j];
+    }
+    for (int s = 0; s < kPackSrc; ++s) t.kof[s][j] = o[s];
+    t.kw[j] = w;
   }
   __syncthreads();
-  const V a = (V)p.a, b = (V)p.b, c = (V)p.c;
+  const V a = (V)p.a, b = (V)p.b, c = (V)p.c, d = (V)p.d;
   // Each thread keeps one index of the unit-stride side fixed (a K column when KF, a row
   // otherwise), so consecutive threads read consecutive addresses, and walks the other
   // side; the fixed side's offsets and bound are read once.  All of a thread's gathers
@@ -541,12 +557,16 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
   const int fx = tid % NF, w0 = tid / NF;
   const bool fx_ok = KF ? (k0 + fx < p.K) : (r0 + fx < p.R);
   const long long wlim = KF ? (p.R - r0) : (p.K - k0);
-  long long f[4] = {0, 0, 0, 0};
+  long long f[kPackSrc] = {0, 0, 0, 0, 0, 0};
   if (p.X) f[0] = KF ? t.kof[0][fx] : t.rof[0][fx];
   if (p.Y) f[1] = KF ? t.kof[1][fx] : t.rof[1][fx];
   if (p.P) {
     f[2] = KF ? t.kof[2][fx] : t.rof[2][fx];
     f[3] = KF ? t.kof[3][fx] : t.rof[3][fx];
+  }
+  if (p.R2) {
+    f[4] = KF ? t.kof[4][fx] : t.rof[4][fx];
+    f[5] = KF ? t.kof[5][fx] : t.rof[5][fx];
   }
   V vals[PER];
 #pragma unroll
@@ -560,6 +580,8 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
       if (p.X) v = a * pack_ld<V>(p.X + f[0] + wof(0));
       if (p.Y) v += b * pack_ld<V>(p.Y + f[1] + wof(1));
       if (p.P) v += c * pack_ld<V>(p.P + f[2] + wof(2)) * pack_ld<V>(p.Q + f[3] + wof(3));
+      if (p.R2) v += d * pack_ld<V>(p.R2 + f[4] + wof(4)) * pack_ld<V>(p.S2 + f[5] + wof(5));
+      if (p.k_w) v *= KF ? t.kw[fx] : t.kw[wv];
     }
     vals[u] = v;
   }
@@ -784,7 +806,7 @@ bool fill_pack(PackIdx& d, int n, const long long* ext, const long long* str) {
   d.n = n ? n : 1;
   for (int q = 0; q < kMaxSub; ++q) {
     d.ext[q] = 1;
-    for (int s = 0; s < 4; ++s) d.s[s][q] = 0;
+    for (int s = 0; s < kPackSrc; ++s) d.s[s][q] = 0;
   }
   for (int q = 0; q < n; ++q) {
     if (ext[q] <= 0 || ext[q] > 0x7fffffffLL) {
@@ -792,7 +814,7 @@ bool fill_pack(PackIdx& d, int n, const long long* ext, const long long* str) {
       return false;
     }
     d.ext[q] = ext[q];
-    for (int s = 0; s < 4; ++s) d.s[s][q] = str[s * kMaxSub + q];
+    for (int s = 0; s < kPackSrc; ++s) d.s[s][q] = str[s * kMaxSub + q];
   }
   return true;
 }
@@ -807,14 +829,18 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
                                 int k_n, const long long* k_ext, const long long* k_str,
                                 long long Kp, double a, const double* X, double b,
                                 const double* Y, double c, const double* P, const double* Q,
-                                void* hi, void* mid, void* lo, float* row_scale,
-                                const long long* row_tab, long long rows, void* stream) {
+                                double d, const double* R, const double* S, void* hi, void* mid,
+                                void* lo, float* row_scale, const long long* row_tab,
+                                long long rows, const long long* k_tab, const float* k_w,
+                                long long kcount, void* stream) {
   PackArgs p{};
   if (!fill_pack(p.r, r_n, r_ext, r_str) || !fill_pack(p.k, k_n, k_ext, k_str)) return -1;
   p.row_tab = row_tab;
+  p.k_tab = k_tab;
+  p.k_w = k_w;
   if (fmt == kBF16x3F || fmt == kBF16x3S) fmt = kBF16x3;  // same pieces; the GEMM differs
-  if (fmt < 0 || fmt > 3 || (!X && !P) || !hi || ((fmt == kBF16x3 || fmt == kBF16x6) && !lo) ||
-      (fmt == kBF16x6 && !mid) || (fmt == kFP8 && !row_scale) || (P && !Q)) {
+  if (fmt < 0 || fmt > 3 || (!X && !P && !R) || !hi || ((fmt == kBF16x3 || fmt == kBF16x6) && !lo) ||
+      (fmt == kBF16x6 && !mid) || (fmt == kFP8 && !row_scale) || (P && !Q) || (R && !S)) {
     set_error("pcg_pack_operand: bad pointers for format %d", fmt);
     return -1;
   }
@@ -829,6 +855,16 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   }
   p.K = 1;
   for (int q = 0; q < p.k.n; ++q) p.K *= p.k.ext[q];
+  if (k_tab) {
+    if (kcount <= 0) {
+      set_error("pcg_pack_operand: a K table needs kcount > 0");
+      return -1;
+    }
+    p.K = kcount;
+  } else if (k_w) {
+    set_error("pcg_pack_operand: K multipliers need a K table");
+    return -1;
+  }
   const int kblk = (fmt == kFP8) ? 128 : 64;
   if (Kp < p.K || Kp % kblk != 0) {
     set_error("pcg_pack_operand: Kp=%lld must be >= K=%lld and a multiple of %d", Kp, p.K, kblk);
@@ -838,21 +874,29 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
   p.a = a;
   p.b = b;
   p.c = c;
+  p.d = d;
   p.X = X;
   p.Y = Y;
   p.P = P;
   p.Q = Q;
+  p.R2 = R;
+  p.S2 = S;
   p.hi = hi;
   p.lo = (fmt == kBF16x3 || fmt == kBF16x6) ? lo : nullptr;
   p.mid = (fmt == kBF16x6) ? mid : nullptr;
   p.scale = row_scale;
   p.fmt = fmt;
   // gather along K when X is at least as contiguous along K as along the rows
+  // (a table-driven side counts as the gathered side unless the other side is a table too;
+  // the caller passes the table's typical step in the unused stride slot then)
   long long ks = 0, rs = 0;
+  const int src0 = X ? 0 : (P ? 2 : 4);
   for (int q = 0; q < p.k.n; ++q)
-    if (p.k.s[0][q] != 0) ks = (ks == 0) ? llabs(p.k.s[0][q]) : std::min(ks, llabs(p.k.s[0][q]));
+    if (p.k.s[src0][q] != 0)
+      ks = (ks == 0) ? llabs(p.k.s[src0][q]) : std::min(ks, llabs(p.k.s[src0][q]));
   for (int q = 0; q < p.r.n; ++q)
-    if (p.r.s[0][q] != 0) rs = (rs == 0) ? llabs(p.r.s[0][q]) : std::min(rs, llabs(p.r.s[0][q]));
+    if (p.r.s[src0][q] != 0)
+      rs = (rs == 0) ? llabs(p.r.s[src0][q]) : std::min(rs, llabs(p.r.s[src0][q]));
   const int kfast = (rs == 0 || (ks != 0 && ks <= rs)) ? 1 : 0;
   const long long gx = (p.R + TR - 1) / TR, gy = Kp / TK;
   if (gy > 65535 || p.R > 0x7fffffffLL - TR) {  // row and K indices stay below 2^31

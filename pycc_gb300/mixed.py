@@ -57,7 +57,8 @@ class MixedResidual:
         self.bad = 0
         self.history = []
         self.profile = None       # list of (subscripts, fmt, start, end) events when set
-        self._pairs = None        # i <= j pair tables of the ladder
+        self._pairs = None        # output map of the i <= j pair terms
+        self._pm = None           # offset tables of the ladder's pair form
         self._hole_tab = None     # the pair columns of Wmnij for the hole ladder
         self._r_seed = None
         self._blocks = None       # the integral blocks the caches were built from
@@ -164,60 +165,133 @@ class MixedResidual:
 
     # -- the <ab|ef> ladder over i <= j pairs (pycc/ccwfn.py:931) ---------------------------
     def _pair_tables(self):
+        """Output map of the i <= j pair terms: the pair columns' offsets in the half
+        residual and their weights (1/2 on i = j, which the symmetrisation doubles)."""
         if self._pairs is None:
             no, nv = self.w.no, self.w.nv
             ii, jj = np.triu_indices(no)
-            tab = np.zeros((4, ii.size), dtype=np.int64)
-            tab[0] = ii * no * nv * nv + jj * nv * nv       # t2[i, j, :, :]
-            tab[2] = ii * nv                                # t1[i, :]
-            tab[3] = jj * nv                                # t1[j, :]
             cmap = (ii * no * nv * nv + jj * nv * nv).astype(np.int64)
             csc = np.where(ii == jj, 0.5, 1.0)
             dev = self.w.device1
-            self._pairs = (torch.from_numpy(tab).to(dev), torch.from_numpy(cmap).to(dev),
-                           torch.from_numpy(csc).to(dev))
+            self._pairs = (torch.from_numpy(cmap).to(dev), torch.from_numpy(csc).to(dev))
         return self._pairs
 
-    def ladder_pairs(self, t1, t2, r, fmt):
-        """r_ijab += 1/2 tau_ijef <ab|ef> through the i <= j pairs only.
+    def _pm_tables(self, t1, t2, V):
+        """Offset tables of the symmetric / antisymmetric pair form of the ladder
+        (``ladder_pm``): rows of V+- over the a <= b / a < b pairs, K over the e <= f /
+        e < f pairs (with 1/2 on e = f for V+, whose <ab|ef> + <ab|fe> doubles it there),
+        rows of T+- over the i <= j / i < j pairs.  Offsets follow the tensors' own strides
+        (V: [a, b, e, f]; t2: [i, j, e, f]; t1: [i, e])."""
+        key = (tuple(V.stride()), tuple(t2.stride()), tuple(t1.stride()))
+        if self._pm is not None and self._pm[0] == key:
+            return self._pm[1]
+        no, nv = self.w.no, self.w.nv
+        dev = self.w.device1
+        sv, s2, s1 = V.stride(), t2.stride(), t1.stride()
+        tabs = {}
+        for sign, k in (("+", 0), ("-", 1)):
+            a, b = np.triu_indices(nv, k)            # a <= b (+) or a < b (-) pairs
+            i, j = np.triu_indices(no, k)
+            vr = np.zeros((6, a.size), dtype=np.int64)
+            vr[0] = vr[1] = a * sv[0] + b * sv[1]
+            vk = np.zeros((6, a.size), dtype=np.int64)          # K pairs: e = a, f = b
+            vk[0] = a * sv[2] + b * sv[3]
+            vk[1] = b * sv[2] + a * sv[3]
+            tr = np.zeros((6, i.size), dtype=np.int64)
+            tr[0] = tr[1] = i * s2[0] + j * s2[1]
+            tr[2] = tr[4] = i * s1[0]                            # t_ie, t_if
+            tr[3] = tr[5] = j * s1[0]                            # t_jf, t_je
+            tk = np.zeros((6, a.size), dtype=np.int64)
+            tk[0] = a * s2[2] + b * s2[3]                        # tau_ijef
+            tk[1] = b * s2[2] + a * s2[3]                        # tau_ijfe
+            tk[2], tk[3] = a * s1[1], b * s1[1]                  # t_ie t_jf
+            tk[4], tk[5] = b * s1[1], a * s1[1]                  # t_if t_je
+            kw = np.where(a == b, 0.5, 1.0).astype(np.float32) if sign == "+" else None
+            t = lambda x: torch.from_numpy(x).to(dev) if x is not None else None
+            tabs[sign] = {"vrow": t(vr), "vk": t(vk), "kw": t(kw), "trow": t(tr), "tk": t(tk),
+                          "rows": a.size, "cols": i.size}
+        self._pm = (key, tabs)
+        return tabs
 
-        tau_jife = tau_ijef and <ba|fe> = <ab|ef>, so the term is symmetric under
-        (i<->j, a<->b) and the symmetrisation r2 = h + h' of r_T2 (ccwfn.py:790) doubles it.
-        Writing the full term for i < j into h (and half of it for i = j) and nothing for
-        i > j gives the same symmetrised residual with o(o+1)/2 instead of o^2 rows.
-        """
+    def ladder_pm(self, t1, t2, r, fmt):
+        """r_ijab += 1/2 tau_ijef <ab|ef> (pycc/ccwfn.py:931) in symmetric / antisymmetric
+        pair form: two GEMMs, G+- = T+- . V+-, over the e <= f (e < f) pairs of K, the
+        a <= b (a < b) pairs of rows and the i <= j (i < j) pairs of columns, then
+        ``pcg_ladder_pm_assemble`` adds S = 1/2 (G+ + sign(b - a) G-) = sum_ef tau_ijef <ab|ef>
+        into the half residual for i < j (twice the term: h_jiba then carries none of it)
+        and S / 2 for i = j, as the i <= j pair form of the ladder does.
+        T+-_ij,ef = tau_ijef +- tau_ijfe (packed from t2 and t1 in one pass), V+-_ab,ef =
+        <ab|ef> +- <ab|fe> (packed once per format and cached).  Half of the i <= j pair
+        form's tensor-core work, and half of its packed integral bytes."""
         if not r.is_contiguous():
-            raise ValueError("ladder_pairs: the half residual must be contiguous")
-        tab, cmap, csc = self._pair_tables()
-        tau = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
-        pb = pack(tau, ['i', 'j'], ['e', 'f'], fmt, self.w.stream, row_tab=tab)
-        pa = self.tc._pack(self.eri('vvvv', 'abef'), ['a', 'b'], ['e', 'f'], fmt, 'A')
-        torch.cuda.nvtx.range_push("ladder")     # selects this launch for profilers
-        self.tc.run_gemm('ijef,abef->ijab', fmt, pa, pb, r, ['a', 'b'], [], 'ijab', 1.0, 1.0,
-                         col_map=cmap, col_scale=csc)
-        torch.cuda.nvtx.range_pop()
+            raise ValueError("ladder_pm: the half residual must be contiguous")
+        no, nv = self.w.no, self.w.nv
+        V = self.w.H.ERI.blocks['vvvv']
+        tabs = self._pm_tables(t1, t2, V)
+        dev = self.w.device1
+        G = {}
+        for sign, c in (("+", 1.0), ("-", -1.0)):
+            tb = tabs[sign]
+            if tb["rows"] == 0 or tb["cols"] == 0:
+                G[sign] = None
+                continue
+            vop = Operand('abef', (V, 'abef'), a=1.0, Y=(V, 'abfe'), b=c,
+                          key=("ERI", "vvvv", sign))
+            pa = self.tc._pack(vop, ['a', 'b'], ['e', 'f'], fmt, 'A', row_tab=tb["vrow"],
+                               k_tab=tb["vk"], k_w=tb["kw"])
+            top = Operand('ijef', (t2, 'ijef'), a=1.0, Y=(t2, 'ijfe'), b=c, P=(t1, 'ie'),
+                          Q=(t1, 'jf'), c=1.0, R=(t1, 'if'), S=(t1, 'je'), d=c)
+            pb = self.tc._pack(top, ['i', 'j'], ['e', 'f'], fmt, 'B', row_tab=tb["trow"],
+                               k_tab=tb["tk"])
+            out = torch.empty((tb["cols"], tb["rows"]), dtype=torch.float64, device=dev)
+            self.tc.run_gemm('ijef,abef->ijab' + sign, fmt, pa, pb, out, ['p'], ['q'], 'qp',
+                             0.5, 0.0)
+            G[sign] = out
+        _lib.call("pcg_ladder_pm_assemble", G["+"].data_ptr(),
+                  G["-"].data_ptr() if G["-"] is not None else None, no, nv, r.data_ptr(),
+                  _lib.stream_handle(self.w.stream))
 
     def hole_ladder_pairs(self, t1, t2, Wmnij, r):
         """r_ijab += 1/2 tau_mnab W_mnij (pycc/ccwfn.py:930) through the i <= j pairs only.
 
         W_nmji = W_mnij and tau_nmba = tau_mnab, so the term is symmetric under
-        (i<->j, a<->b), as the particle ladder is: the same output map and 1/2 diagonal weights
-        (``ladder_pairs``) apply, with a row table selecting the pair columns of W_mnij.
+        (i<->j, a<->b), as the particle ladder is: the i <= j output map and 1/2 diagonal
+        weights of ``_pair_tables`` apply, with a row table selecting the pair columns of
+        W_mnij (offsets from W_mnij's own strides, so any layout of it is read correctly).
         """
+        if not r.is_contiguous():
+            raise ValueError("hole_ladder_pairs: the half residual must be contiguous")
         no = self.w.no
-        if self._hole_tab is None:
+        sw = tuple(Wmnij.stride())
+        if self._hole_tab is None or self._hole_tab[0] != sw:
             ii, jj = np.triu_indices(no)
-            tab = np.zeros((4, ii.size), dtype=np.int64)
-            tab[0] = ii * no + jj                        # Wmnij[m, n, i, j]
-            self._hole_tab = torch.from_numpy(tab).to(self.w.device1)
-        _, cmap, csc = self._pair_tables()
+            tab = np.zeros((6, ii.size), dtype=np.int64)
+            tab[0] = ii * sw[2] + jj * sw[3]             # Wmnij[m, n, i, j]
+            self._hole_tab = (sw, torch.from_numpy(tab).to(self.w.device1))
+        cmap, csc = self._pair_tables()
         fmt = self.fmt()
         tau = Operand('mnab', (t2, 'mnab'), P=(t1, 'ma'), Q=(t1, 'nb'), c=1.0)
         pa = self.tc._pack(tau, ['a', 'b'], ['m', 'n'], fmt, 'A')
         pb = pack(Operand.of('mnij', Wmnij), ['i', 'j'], ['m', 'n'], fmt, self.w.stream,
-                  row_tab=self._hole_tab)
+                  row_tab=self._hole_tab[1])
         self.tc.run_gemm('mnab,mnij->ijab', fmt, pa, pb, r, ['a', 'b'], [], 'ijab', 1.0, 1.0,
                          col_map=cmap, col_scale=csc)
+
+    def timed(self, name, fn, *args):
+        """Run one term; with ``self.profile`` set, CUDA events on the launching stream
+        around it (pack + GEMM + assembly) join the per-term table, and an NVTX range names
+        it for profilers."""
+        torch.cuda.nvtx.range_push(name)
+        if self.profile is None:
+            fn(*args)
+        else:
+            st = torch.cuda.current_stream() if self.w.stream is None else self.w.stream
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            fn(*args)
+            e1.record(st)
+            self.profile.append((name, self.fmt(), e0, e1))
+        torch.cuda.nvtx.range_pop()
 
     # -- intermediates (pycc/ccwfn.py:458-715) -------------------------------------------
     def build_Fae(self, F, t1, t2):
@@ -313,8 +387,8 @@ class MixedResidual:
         contract_f64('je,me->mj', t1, Fme, out=Fmj, alpha=0.5, beta=1.0)
         self.tcc('imab,mj->ijab', Operand.of('imab', t2), Operand.of('mj', Fmj), r, alpha=-1.0)
         # ladders
-        self.hole_ladder_pairs(t1, t2, Wmnij, r)
-        self.ladder_pairs(t1, t2, r, self.ladder_fmt())
+        self.timed("mnab,mnij->ijab", self.hole_ladder_pairs, t1, t2, Wmnij, r)
+        self.timed("ijef,abef->ijab", self.ladder_pm, t1, t2, r, self.ladder_fmt())
         # - t_ma (Z_mbij + <mb|ij>) - t_ie t_ma <mb|ej> - t_ie t_mb <ma|je>, the last written
         # as its (i<->j, a<->b) image - t_je t_ma <mb|ie>, which the symmetrisation
         # r2 = h + h' sums to the same residual; the o^3 v tensors are summed in Zmbij

@@ -4,9 +4,10 @@ A contraction ``out = beta*out + alpha * einsum('A,B->C', opA, opB)`` is execute
 
 1. pack: each operand is gathered from its FP64 source(s) into a K-major row matrix
    ``[rows][Kp]`` in the GEMM's input format (BF16, BF16 hi+lo pair, or FP8 E4M3 with a
-   per-row scale).  An operand may be a combination ``a*X + b*Y + c*P*Q`` of strided FP64
-   tensors (e.g. ``2 t2 - t2.swapaxes(2,3)`` or ``t2 + t1 (x) t1``), so the
-   combinations, index permutations and the conversion happen in one pass;
+   per-row scale).  An operand may be a combination ``a*X + b*Y + c*P*Q + d*R*S`` of strided
+   FP64 tensors (e.g. ``2 t2 - t2.swapaxes(2,3)``, ``t2 + t1 (x) t1``, or tau_ijef + tau_ijfe),
+   so the combinations, index permutations and the conversion happen in one pass; rows and
+   K may also be selected by explicit offset tables (index pairs such as i <= j);
 2. GEMM: 128 x BN tiles on tcgen05 with TMEM accumulators; the epilogue writes FP64 with
    the output permutation expressed as per-row / per-column offsets.
 
@@ -42,16 +43,17 @@ MAX_SUB = 4
 
 
 class Operand:
-    """``a*X + b*Y + c*P*Q`` over the index labels ``labels``.
+    """``a*X + b*Y + c*P*Q + d*R*S`` over the index labels ``labels``.
 
     Each component is ``(tensor, labels)``; labels of the operand a component lacks are
     broadcast (stride 0).
     """
 
-    def __init__(self, labels, X, a=1.0, Y=None, b=0.0, P=None, Q=None, c=0.0, key=None):
+    def __init__(self, labels, X, a=1.0, Y=None, b=0.0, P=None, Q=None, c=0.0, R=None, S=None,
+                 d=0.0, key=None):
         self.labels = labels
-        self.a, self.b, self.c = a, b, c
-        self.X, self.Y, self.P, self.Q = X, Y, P, Q
+        self.a, self.b, self.c, self.d = a, b, c, d
+        self.X, self.Y, self.P, self.Q, self.R, self.S = X, Y, P, Q, R, S
         self.key = key            # cache key for static operands (None = dynamic)
 
     @staticmethod
@@ -59,7 +61,7 @@ class Operand:
         return Operand(labels, (t, labels), key=key)
 
     def sources(self):
-        return [self.X, self.Y, self.P, self.Q]
+        return [self.X, self.Y, self.P, self.Q, self.R, self.S]
 
     def extents(self):
         ext = {}
@@ -83,7 +85,7 @@ class Operand:
         return out
 
     def device(self):
-        return self.X[0].device
+        return next(s for s in self.sources() if s is not None)[0].device
 
 
 def _merge_multi(groups):
@@ -120,18 +122,31 @@ def kblock(fmt):
     return 128 if fmt == FMT_FP8 else 64
 
 
-def pack(op: Operand, row_labels, k_labels, fmt, stream=None, row_tab=None) -> Packed:
+NSRC = 6   # sources of a packed operand: X, Y, P, Q, R, S
+
+
+def pack(op: Operand, row_labels, k_labels, fmt, stream=None, row_tab=None, k_tab=None,
+         k_w=None) -> Packed:
     """Pack ``op`` with rows over ``row_labels`` (or the explicit per-source row offsets
-    ``row_tab``, an int64 [4, R] device tensor) and K over ``k_labels``."""
+    ``row_tab``, an int64 [6, R] device tensor) and K over ``k_labels`` (or the per-source K
+    offsets ``k_tab``, int64 [6, K], with optional float32 K multipliers ``k_w``).  With a
+    table the labels' strides still tell the kernel which side is unit-stride."""
     fmt = pack_format(fmt)
     ext = op.extents()
     rows = [(ext[c], op.strides(c)) for c in row_labels]
     ks = [(ext[c], op.strides(c)) for c in k_labels]
     R = math.prod(ext[c] for c in row_labels) if row_tab is None else int(row_tab.shape[1])
-    K = math.prod(ext[c] for c in k_labels)
+    K = math.prod(ext[c] for c in k_labels) if k_tab is None else int(k_tab.shape[1])
     rows, ks = _merge_multi(rows), _merge_multi(ks)
     if len(rows) > MAX_SUB or len(ks) > MAX_SUB:
         raise ValueError("pack: more than %d sub-indices" % MAX_SUB)
+    for tab in (row_tab, k_tab):
+        if tab is not None and (tab.dtype != torch.int64 or tab.shape[0] != NSRC
+                                or not tab.is_contiguous()):
+            raise ValueError("pack: offset tables are contiguous int64 [%d, n] tensors" % NSRC)
+    if k_w is not None and (k_tab is None or k_w.dtype != torch.float32
+                            or k_w.numel() != K or not k_w.is_contiguous()):
+        raise ValueError("pack: K multipliers need a K table and K float32 entries")
     kb = kblock(fmt)
     Kp = ((K + kb - 1) // kb) * kb
     dev = op.device()
@@ -148,21 +163,22 @@ def pack(op: Operand, row_labels, k_labels, fmt, stream=None, row_tab=None) -> P
 
     def flat(groups):
         e = [g[0] for g in groups]
-        st = [0] * (4 * MAX_SUB)
+        st = [0] * (NSRC * MAX_SUB)
         for q, (_, s) in enumerate(groups):
-            for src in range(4):
+            for src in range(NSRC):
                 st[src * MAX_SUB + q] = s[src]
         return len(groups), _lib.i64s(e), _lib.i64s(st)
+
+    def ptr(t):
+        return t.data_ptr() if t is not None else None
 
     rn, re_, rs = flat(rows)
     kn, ke, kst = flat(ks)
     _lib.call("pcg_pack_operand", int(fmt), rn, re_, rs, kn, ke, kst, Kp,
               float(op.a), _ptr(op.X), float(op.b), _ptr(op.Y), float(op.c), _ptr(op.P),
-              _ptr(op.Q), hi.data_ptr(), mid.data_ptr() if mid is not None else None,
-              lo.data_ptr() if lo is not None else None,
-              scale.data_ptr() if scale is not None else None,
-              row_tab.data_ptr() if row_tab is not None else None,
-              R if row_tab is not None else 0, _lib.stream_handle(stream))
+              _ptr(op.Q), float(op.d), _ptr(op.R), _ptr(op.S), hi.data_ptr(), ptr(mid), ptr(lo),
+              ptr(scale), ptr(row_tab), R if row_tab is not None else 0, ptr(k_tab), ptr(k_w),
+              K if k_tab is not None else 0, _lib.stream_handle(stream))
     return Packed(fmt, R, Kp, hi, lo, scale, mid)
 
 
@@ -255,27 +271,30 @@ class TCEngine:
             self.timing.append({"subs": subscripts, "fmt": fmt, "M": pa.rows, "N": pb.rows,
                                 "Kp": pa.Kp, "start": ev[0], "end": ev[1]})
 
-    def _pack(self, op, rows, ks, fmt, side):
+    def _pack(self, op, rows, ks, fmt, side, row_tab=None, k_tab=None, k_w=None):
+        tabs = tuple(t.data_ptr() if t is not None else None for t in (row_tab, k_tab, k_w))
         if op.key is None:
             if self.dyn_cache is None:
-                return pack(op, rows, ks, fmt, self.stream)
+                return pack(op, rows, ks, fmt, self.stream, row_tab, k_tab, k_w)
             src = tuple((s[0].data_ptr(), tuple(s[0].stride()), s[1]) if s is not None else None
                         for s in op.sources())
-            dkey = (src, op.a, op.b, op.c, op.labels, tuple(rows), tuple(ks), pack_format(fmt))
+            dkey = (src, op.a, op.b, op.c, op.d, op.labels, tuple(rows), tuple(ks), tabs,
+                    pack_format(fmt))
             hit = self.dyn_cache.get(dkey)
             if hit is None:
-                # the entry holds its source tensors, so no later tensor can reuse their
-                # addresses while the cache lives
-                hit = (pack(op, rows, ks, fmt, self.stream),
-                       [s[0] for s in op.sources() if s is not None])
+                # the entry holds its source tensors and tables, so no later tensor can reuse
+                # their addresses while the cache lives
+                hit = (pack(op, rows, ks, fmt, self.stream, row_tab, k_tab, k_w),
+                       [s[0] for s in op.sources() if s is not None] + [row_tab, k_tab, k_w])
                 self.dyn_cache[dkey] = hit
             return hit[0]
-        # the operand's own label string fixes which tensor axis each label names
+        # the operand's own label string fixes which tensor axis each label names; the key
+        # (op.key) names the static tensor and any tables that select from it
         sf = static_pack_format(fmt)
         key = (op.key, op.labels, tuple(rows), tuple(ks), sf)
         p = self.cache.get(key)
         if p is None:
-            p = pack(op, rows, ks, sf, self.stream)
+            p = pack(op, rows, ks, sf, self.stream, row_tab, k_tab, k_w)
             self.cache[key] = p
         return p
 

@@ -152,18 +152,21 @@ class ABIModel:
         return off
 
     def pack_operand(self, fmt, r_n, r_ext, r_str, k_n, k_ext, k_str, Kp, a, X, b, Y, c, P, Q,
-                     hi, mid, lo, scale, row_tab, rows, _st):
+                     d, R_, S_, hi, mid, lo, scale, row_tab, rows, k_tab, k_w, kcount, _st):
         re_, ke = _ints(r_ext, r_n), _ints(k_ext, k_n)
-        rs, ks = _ints(r_str, 16), _ints(k_str, 16)
-        K = int(np.prod(ke)) if ke else 1
+        rs, ks = _ints(r_str, 24), _ints(k_str, 24)
+        K = kcount if k_tab else (int(np.prod(ke)) if ke else 1)
         assert K <= Kp and Kp % (128 if fmt == 2 else 64) == 0
+        assert not k_w or k_tab
         if row_tab:
-            tab = flat(row_tab, 4 * rows, np.int64).reshape(4, rows)
+            rtab = flat(row_tab, 6 * rows, np.int64).reshape(6, rows)
+        if k_tab:
+            ktab = flat(k_tab, 6 * kcount, np.int64).reshape(6, kcount)
         R = rows if row_tab else (int(np.prod(re_)) if re_ else 1)
 
         def source(s, ptr):
-            koff = self._offsets(ke, ks[4 * s:4 * s + k_n])
-            roff = tab[s] if row_tab else self._offsets(re_, rs[4 * s:4 * s + r_n])
+            koff = ktab[s] if k_tab else self._offsets(ke, ks[4 * s:4 * s + k_n])
+            roff = rtab[s] if row_tab else self._offsets(re_, rs[4 * s:4 * s + r_n])
             idx = roff[:, None] + koff[None, :]
             return flat(ptr, int(idx.max()) + 1)[idx]
 
@@ -174,6 +177,10 @@ class ABIModel:
             v += b * source(1, Y)
         if P:
             v += c * source(2, P) * source(3, Q)
+        if R_:
+            v += d * source(4, R_) * source(5, S_)
+        if k_w:
+            v *= flat(k_w, K, np.float32).astype(np.float64)[None, :]
         self.packs[hi] = v
 
     def tc_gemm(self, fmt, A_hi, A_mid, A_lo, M, lda, B_hi, B_mid, B_lo, N, ldb, Kp, a_scale,
@@ -196,6 +203,28 @@ class ABIModel:
         Cf = flat(Cp, int(idx.max()) + 1)
         Cf[idx] = S if beta == 0.0 else beta * Cf[idx] + S
 
+
+    def ladder_pm_assemble(self, Gp, Gm, no, nv, h, _st):
+        """h[i,j,a,b] += G+ (+-) G- over the a <= b triangle of the pairs (i <= j) and their
+        transposed pairs, as pcg_ladder_pm_assemble documents."""
+        P, Q = nv * (nv + 1) // 2, nv * (nv - 1) // 2
+        gp = flat(Gp, (no * (no + 1) // 2) * P).reshape(-1, P)
+        gm = flat(Gm, (no * (no - 1) // 2) * Q).reshape(-1, Q) if Gm else None
+        H = view(h, (no, no, nv, nv), (no * nv * nv, nv * nv, nv, 1))
+        a, b = np.triu_indices(nv)
+        strict = b > a
+        qm = 0
+        for q, (i, j) in enumerate(zip(*np.triu_indices(no))):
+            g = gp[q].copy()
+            if j > i:
+                m = np.zeros(P)
+                if gm is not None:
+                    m[strict] = gm[qm]
+                qm += 1
+                H[i, j][a, b] += g + m
+                H[j, i][a[strict], b[strict]] += (g - m)[strict]
+            else:
+                H[i, i][a, b] += np.where(strict, g, 0.5 * g)
 
     # -- the (T) entry points ------------------------------------------------------------------
     PART_LEN = 4              # the model's per-triple partial-sum length in FP32 mode

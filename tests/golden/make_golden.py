@@ -3,7 +3,7 @@
 The reference (CrawfordGroup/pycc) is pure Python.  Its integral source needs psi4 and
 qcelemental, which are not installed, but the CCSD arithmetic never touches them: this
 script puts inert stand-ins for both modules into ``sys.modules``, imports ``pycc`` from
-the reference tree (``$PYCC_REF``, default ``/root/reference``), and assembles a ``CCwfn``
+the reference tree named by ``$PYCC_REF`` (required), and assembles a ``CCwfn``
 with ``CCwfn.__new__`` plus the attributes that ``CCwfn.__init__`` would have set
 (``pycc/ccwfn.py:76-213``, ``pycc/wavefunction.py:293-332``), on the synthetic
 Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
@@ -12,7 +12,7 @@ Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
 
 Usage::
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian] [--no-complex]
+    PYCC_REF=<reference tree> PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian] [--no-complex]
 
 The no=20, nv=180 fixtures need ~30 GB of host RAM and several minutes.
 """
@@ -33,70 +33,19 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
 from pycc_gb300.synth import SyntheticFactors, WORKLOADS  # noqa: E402
+from oracle import reference as _ref  # noqa: E402
 
 
 def import_reference():
-    ref = os.environ.get("PYCC_REF", "/root/reference")
-    sys.dont_write_bytecode = True
-    for name in ("psi4", "qcelemental"):
-        if name not in sys.modules:
-            mod = types.ModuleType(name)
-            consts = types.SimpleNamespace(get=lambda *a, **k: 1.0,
-                                           conversion_factor=lambda *a, **k: 1.0)
-            mod.constants = consts
-            mod.core = types.SimpleNamespace()
-            sys.modules[name] = mod
-    sys.path.insert(0, ref)
-    import pycc  # noqa: F401
-    return pycc
+    """The reference package from ``$PYCC_REF`` (its source tree), with psi4 / qcelemental
+    stand-ins (``oracle.reference.import_reference``)."""
+    ref = os.environ.get("PYCC_REF")
+    if not ref:
+        raise SystemExit("make_golden.py: set PYCC_REF to the reference's source tree")
+    return _ref.import_reference(ref)
 
 
-class _H:
-    pass
-
-
-def make_ref_ccwfn(pycc, F, ERI, L, no, nv, model="CCSD"):
-    from pycc.ccwfn import CCwfn
-    from pycc.device import DeviceManager
-    w = CCwfn.__new__(CCwfn)
-    w.model = model
-    w.method = model
-    w.orbital_basis = "spatial"
-    w.local = None
-    w.need_singles = ['CCSD', 'CCSD(T)', 'CC2', 'CC3']
-    w.make_t3_density = False
-    w.store_triples = False
-    w.real_time = False
-    w.field = False
-    w.nfzc = 0
-    w.no, w.nv, w.nmo = no, nv, no + nv
-    w.o = slice(0, no)
-    w.v = slice(no, no + nv)
-    H = _H()
-    H.F = F
-    H.eps = np.diag(F).copy()
-    H.ERI = ERI
-    H.L = L
-    w.H = H
-    w.eref = 0.0
-    mgr = DeviceManager('CPU', 'DP')
-    w.device_manager = mgr
-    w.contract = mgr.contract
-    w.precision = 'DP'
-    w.device = 'CPU'
-    w.device0 = None
-    w.device1 = None
-    w.e_conv = 1e-7
-    w.r_conv = 1e-7
-    w.maxiter = 100
-    o, v = w.o, w.v
-    eps_o, eps_v = H.eps[o], H.eps[v]
-    w.Dijab = (eps_o.reshape(-1, 1, 1, 1) + eps_o.reshape(-1, 1, 1)
-               - eps_v.reshape(-1, 1) - eps_v)
-    w.Dia = eps_o.reshape(-1, 1) - eps_v
-    w.t1 = np.zeros((no, nv))
-    w.t2 = ERI[o, o, v, v].copy() / w.Dijab
-    return w
+make_ref_ccwfn = _ref.make_ref_ccwfn
 
 
 def probe_amplitudes(no, nv, t2_mp2, seed):

@@ -36,7 +36,7 @@ def test_library_exports_all(lib):
 
 
 def test_abi_version(lib):
-    assert lib.pcg_abi_version() == 1
+    assert lib.pcg_abi_version() == 2
 
 
 @pytest.mark.skipif(__import__("torch").cuda.is_available(),

@@ -192,3 +192,90 @@ def test_mixed_ragged_vs_oracle(cuda, no, nv):
     torch.cuda.synchronize()
     assert np.abs(r2.cpu().numpy() - r2o).max() / np.abs(r2o).max() < 1e-4
     assert np.abs(r1.cpu().numpy() - r1o).max() / np.abs(r1o).max() < 1e-4
+
+
+def test_pack_tables_and_second_product(cuda):
+    """a*X + b*Y + c*P*Q + d*R*S with explicit row and K offset tables and K multipliers
+    (the pair form of the ladder: T+_ij,ef = tau_ijef + tau_ijfe over i <= j, e <= f),
+    against FP64 within the FP32 rounding of the operands."""
+    import numpy as np
+    from pycc_gb300.tc import pack
+    g = torch.Generator(device=cuda).manual_seed(13)
+    no, nv = 5, 23
+    t2 = torch.randn(no, no, nv, nv, generator=g, device=cuda, dtype=torch.float64)
+    t1 = torch.randn(no, nv, generator=g, device=cuda, dtype=torch.float64)
+    i, j = np.triu_indices(no)
+    e, f = np.triu_indices(nv)
+    s2, s1 = t2.stride(), t1.stride()
+    rt = np.zeros((6, i.size), dtype=np.int64)
+    rt[0] = rt[1] = i * s2[0] + j * s2[1]
+    rt[2] = rt[4] = i * s1[0]
+    rt[3] = rt[5] = j * s1[0]
+    kt = np.zeros((6, e.size), dtype=np.int64)
+    kt[0], kt[1] = e * s2[2] + f * s2[3], f * s2[2] + e * s2[3]
+    kt[2], kt[3], kt[4], kt[5] = e, f, f, e
+    kw = np.where(e == f, 0.5, 1.0).astype(np.float32)
+    op = Operand("ijef", (t2, "ijef"), a=1.0, Y=(t2, "ijfe"), b=-1.0, P=(t1, "ie"), Q=(t1, "jf"),
+                 c=1.0, R=(t1, "if"), S=(t1, "je"), d=-1.0)
+    tt = lambda x: torch.from_numpy(x).to(cuda)
+    P = pack(op, ["i", "j"], ["e", "f"], FMT_BF16X3, row_tab=tt(rt), k_tab=tt(kt), k_w=tt(kw))
+    torch.cuda.synchronize()
+    tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
+    I, J, E, Fi = (torch.from_numpy(x).to(cuda) for x in (i, j, e, f))
+    ref = (tau[I[:, None], J[:, None], E[None, :], Fi[None, :]]
+           - tau[I[:, None], J[:, None], Fi[None, :], E[None, :]]) * tt(kw).double()[None, :]
+    K = e.size
+    got = P.hi[:, :K].double() + P.lo[:, :K].double()
+    assert got.shape == ref.shape
+    assert torch.all((got - ref).abs() <= 2.0 ** -16 * ref.abs() + 2.0 ** -19)
+    assert torch.all(P.hi[:, K:].float() == 0)
+
+
+def _ladder_setup(cuda, no, nv, integer=False, seed=3):
+    g = torch.Generator(device=cuda).manual_seed(seed)
+    if integer:
+        V = torch.randint(-2, 3, (nv, nv, nv, nv), generator=g, device=cuda).double()
+        t2 = torch.randint(-2, 3, (no, no, nv, nv), generator=g, device=cuda).double()
+        t1 = torch.randint(-1, 2, (no, nv), generator=g, device=cuda).double()
+    else:
+        V = torch.randn(nv, nv, nv, nv, generator=g, device=cuda, dtype=torch.float64)
+        t2 = 0.1 * torch.randn(no, no, nv, nv, generator=g, device=cuda, dtype=torch.float64)
+        t1 = 0.1 * torch.randn(no, nv, generator=g, device=cuda, dtype=torch.float64)
+    V = V + V.permute(1, 0, 3, 2)              # <ab|ef> = <ba|fe>
+    t2 = t2 + t2.permute(1, 0, 3, 2)           # t2_ijab = t2_jiba
+    tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
+    ref = 0.5 * torch.einsum("ijef,abef->ijab", tau, V)
+    ref = ref + ref.permute(1, 0, 3, 2)        # through the symmetrisation
+    return V, t1, t2.contiguous(), ref
+
+
+def _ladder_run(cuda, V, t1, t2, fmt):
+    from types import SimpleNamespace
+    from pycc_gb300.mixed import MixedResidual
+    no, nv = t1.shape
+    w = SimpleNamespace(device1=cuda, stream=None, no=no, nv=nv, vvvv_fp8=True,
+                        switch_threshold=1e-5,
+                        H=SimpleNamespace(ERI=SimpleNamespace(blocks={"vvvv": V})))
+    eng = MixedResidual(w)
+    h = torch.zeros(no, no, nv, nv, dtype=torch.float64, device=cuda)
+    eng.ladder_pm(t1, t2, h, fmt)
+    torch.cuda.synchronize()
+    eng.tc.check_status()
+    return h + h.permute(1, 0, 3, 2)
+
+
+@pytest.mark.parametrize("no,nv", [(4, 24), (5, 37), (1, 9)])
+def test_ladder_pair_form_exact_integers(cuda, no, nv):
+    """The symmetric / antisymmetric pair form of the <ab|ef> ladder is exact on integer data
+    in BF16 (every packed value and partial sum is an integer below 2^24)."""
+    V, t1, t2, ref = _ladder_setup(cuda, no, nv, integer=True)
+    got = _ladder_run(cuda, V, t1, t2, FMT_BF16)
+    assert torch.equal(got, ref)
+
+
+@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3F, FMT_BF16X3S, FMT_FP8])
+def test_ladder_pair_form_random(cuda, fmt):
+    """The ladder's pair form in each format against FP64, within the format's bound."""
+    V, t1, t2, ref = _ladder_setup(cuda, 6, 45)
+    got = _ladder_run(cuda, V, t1, t2, fmt)
+    assert frob(got, ref) < TOL[fmt]

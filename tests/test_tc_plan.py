@@ -15,7 +15,7 @@ from pycc_gb300.tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_B
 def recorder(monkeypatch):
     calls = {"pack": [], "gemm": []}
 
-    def fake_pack(op, rows, ks, fmt, stream=None, row_tab=None):
+    def fake_pack(op, rows, ks, fmt, stream=None, row_tab=None, k_tab=None, k_w=None):
         ext = op.extents()
         R = 1
         for c in rows:
