@@ -189,8 +189,9 @@ int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const long long* 
  *   format as above, plus 4 = split-BF16x3 fused (both pieces of A and B loaded per stage,
  *   the three products issued from it; faster, with a slightly larger FP32 truncation bias),
  *   5 = split-BF16x3 fused with the small products and the leading product in separate
- *   FP32 accumulators added once per chunk (the accuracy of 1, the traffic of 4; N tiles
- *   of at most 128 columns),
+ *   FP32 accumulators (the leading one flushed per K chunk, the small one once per tile,
+ *   added together before the FP64 accumulate: the accuracy of 1, the traffic of 4; N
+ *   tiles of at most 160 columns),
  *   1 = three tcgen05 passes Al.Bh + Ah.Bl + Ah.Bh, 3 = the six piece
  *   products of order <= 2^-16 (smallest first), 2 = FP8 with the row scales applied in the
  *   epilogue.  off_m / off_n: flat index over up to 4 sub-indices (extents, element strides

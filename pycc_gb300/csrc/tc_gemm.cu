@@ -23,6 +23,7 @@
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 #include <algorithm>
+#include <cmath>
 
 namespace pcg {
 namespace tc {
@@ -53,6 +54,7 @@ struct EpiIdx {
 struct Args {
   long long M, N;
   long long mt, nt;  // output tiles along M and N
+  int gm;            // M tiles per raster group (see decode_tile)
   int splits;        // K splits across CTAs (FP64 atomics in the epilogue when > 1)
   int kb_per_split;  // K blocks of one split
   int nkb_total;     // K blocks of the whole K range
@@ -101,7 +103,10 @@ constexpr int GEMM_THREADS = 64 + 32 * GEMM_EPI_WARPS;
 // TMEM accumulator of their own, the leading Ah.Bh in another, and the epilogue adds them
 // once.  The small corrections then never meet the leading term's magnitude inside the
 // truncating FP32 accumulator (the by-pass format's accuracy, at the fused format's
-// traffic); four BN-column accumulators (two buffers) limit BN to 128.
+// traffic).  The small products are about 2^-8 of the leading one, so their accumulator
+// runs over the tile's whole K range without the chunked FP64 flushes the leading product
+// needs: one BN-column region for them next to the two BN-column leading buffers, which
+// limits BN to 160 (480 of the 512 TMEM columns).
 template <int BN, int NP = 1, bool SPLIT = false>
 struct Smem {
   static constexpr int A_BYTES = BM * KBYTES;
@@ -112,21 +117,29 @@ struct Smem {
   static constexpr int FIT = (kSmemMax - 1024 - TAIL) / STAGE;
   static constexpr int STAGES = FIT > 8 ? 8 : FIT;
   static constexpr int TOTAL = 1024 /*align*/ + STAGES * STAGE + TAIL;
-  static constexpr int ACC = SPLIT ? 2 * BN : BN;  // TMEM columns of one buffer
-  static constexpr unsigned TMEM_COLS = (2 * ACC <= 128) ? 128 : ((2 * ACC <= 256) ? 256 : 512);
+  static constexpr int ACC = BN;                        // TMEM columns of one buffer
+  static constexpr int SMALL = 2 * BN;                  // SPLIT: small-product region
+  static constexpr int USED = SPLIT ? 3 * BN : 2 * BN;
+  static constexpr unsigned TMEM_COLS = (USED <= 128) ? 128 : ((USED <= 256) ? 256 : 512);
   static_assert(BN % 32 == 0 && BN >= 64 && BN <= 256, "BN: multiple of 32 in [64, 256]");
-  static_assert(2 * ACC <= 512 && (!SPLIT || NP == 2), "TMEM holds 512 columns");
+  static_assert(USED <= 512 && (!SPLIT || NP == 2), "TMEM holds 512 columns");
   static_assert(STAGES >= 2, "shared-memory ring too shallow");
 };
 
-// Tile t -> (split, m tile, n tile); N tiles fastest so CTAs running together share A.
+// Tile t -> (split, m tile, n tile).  Tiles are walked in groups of gm M tiles: within a
+// group the M tile runs fastest, then the N tile, so the CTAs of one wave (consecutive t)
+// cover about gm M tiles x (wave / gm) N tiles and share both operands' row blocks in L2.
+// gm = 1 is the N-fastest order.  The host picks gm per launch.
 __device__ __forceinline__ void decode_tile(const Args& p, long long t, int& split, long long& m0,
                                             long long& n0) {
   const long long per = p.mt * p.nt;
   split = (int)(t / per);
   const long long r = t % per;
-  m0 = (r / p.nt) * BM;
-  n0 = (r % p.nt);
+  const long long group = r / ((long long)p.gm * p.nt);
+  const long long rg = r % ((long long)p.gm * p.nt);
+  const long long gm_here = min((long long)p.gm, p.mt - group * p.gm);
+  m0 = (group * p.gm + rg % gm_here) * BM;
+  n0 = rg / gm_here;
 }
 
 // One batch of W (16 or 32) accumulator columns of this thread's output row: every old C
@@ -151,17 +164,19 @@ template <int W, bool SPLIT = false>
 __device__ __forceinline__ void epi_batch(uint32_t taddr, const int* co, const float* sc,
                                           bool row_ok, double* crow, float ascale,
                                           double cscale, bool need_old, int atomic_out,
-                                          uint32_t lead_off = 0) {
+                                          uint32_t small_addr = 0, bool add_small = false) {
   uint32_t r[W];
   if constexpr (W == 32) tmem_ld32(taddr, r);
   else tmem_ld16(taddr, r);
-  if constexpr (SPLIT) {  // small-product sum + leading-product sum, one FP32 rounding
-    uint32_t r2[W];
-    if constexpr (W == 32) tmem_ld32(taddr + lead_off, r2);
-    else tmem_ld16(taddr + lead_off, r2);
+  if constexpr (SPLIT) {
+    if (add_small) {  // leading chunk sum + the tile's small-product sum, one FP32 rounding
+      uint32_t r2[W];
+      if constexpr (W == 32) tmem_ld32(small_addr, r2);
+      else tmem_ld16(small_addr, r2);
 #pragma unroll
-    for (int j = 0; j < W; ++j)
-      r[j] = __float_as_uint(__uint_as_float(r[j]) + __uint_as_float(r2[j]));
+      for (int j = 0; j < W; ++j)
+        r[j] = __float_as_uint(__uint_as_float(r[j]) + __uint_as_float(r2[j]));
+    }
   }
   if (!row_ok) return;
   int cj[W];
@@ -207,7 +222,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
   uint64_t* empty = full + S;
   uint64_t* tfull = empty + S;   // [2] accumulator ready (MMA -> epilogue)
   uint64_t* tempty = tfull + 2;  // [2] accumulator drained (epilogue -> MMA)
-  uint64_t* mdone = tempty + 2;  // all MMAs of this CTA retired
+  uint64_t* sempty = tempty + 2; // SPLIT: small-product region drained (epilogue -> MMA)
+  uint64_t* mdone = sempty + 1;  // all MMAs of this CTA retired
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mdone + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   constexpr int HB = BN / 2;  // columns drained by one epilogue warp
@@ -227,6 +243,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       mbar_init(&tfull[b], 1);
       mbar_init(&tempty[b], GEMM_EPI_WARPS);
     }
+    mbar_init(sempty, GEMM_EPI_WARPS);
     mbar_init(mdone, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -291,14 +308,32 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       // ---- MMA issuer ----
       uint32_t idesc = (1u << 4) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
       if (!p.fp8) idesc |= (1u << 7) | (1u << 10);  // A, B = BF16 (FP8 E4M3 encodes as 0)
-      int it = 0, u = 0;
+      int it = 0, u = 0, tl = 0;
       bool stop = false;
-      for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x) {
+      const uint32_t tsmall = tmem + (uint32_t)L::SMALL;
+      for (long long t = blockIdx.x; t < ntiles && !stop; t += gridDim.x, ++tl) {
         int split;
         long long m0, nti;
         decode_tile(p, t, split, m0, nti);
         const int kb0 = split * p.kb_per_split;
         const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
+        uint32_t acc_small = 0u;
+        if (SPLIT && tl >= 1) {  // the previous tile's small-product sum has been read
+          if (!mbar_wait(&sempty[0], (tl - 1) & 1)) {
+            atomicExch(p.status, kStatusTimeoutEmpty);
+            *abort_flag = 1;
+          }
+          if (*abort_flag) {
+            stop = true;
+            break;
+          }
+          tc_fence_after();
+        }
+        // the last N tile of a ragged N multiplies only its present columns (rounded up to
+        // the MMA's multiple of 16); the columns beyond are never stored
+        const long long nleft = p.N - nti * BN;
+        const uint32_t nmma = nleft >= BN ? (uint32_t)BN : (uint32_t)((nleft + 15) & ~15LL);
+        const uint32_t idesc_t = (idesc & ~(0x3Fu << 17)) | ((nmma >> 3) << 17);
         for (int c0 = kb0; c0 < kb1 && !stop; c0 += p.kb_chunk, ++u) {
           const int c1 = min(c0 + p.kb_chunk, kb1);
           const int b = u & 1;
@@ -312,7 +347,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           }
           tc_fence_after();
           const uint32_t d = tmem + (uint32_t)(b * L::ACC);
-          uint32_t acc = 0u, acc_lead = 0u;
+          uint32_t acc = 0u;
           const int npass = (NP == 1) ? p.npass : 1;
           for (int pass = 0; pass < npass && !stop; ++pass) {
             for (int kb = c0; kb < c1; ++kb, ++it) {
@@ -332,9 +367,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
 #pragma unroll
                 for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per 128-byte stage row
                   if (p.fp8)
-                    umma_f8(d, da + 2 * k, db + 2 * k, idesc, acc);
+                    umma_f8(d, da + 2 * k, db + 2 * k, idesc_t, acc);
                   else
-                    umma_f16(d, da + 2 * k, db + 2 * k, idesc, acc);
+                    umma_f16(d, da + 2 * k, db + 2 * k, idesc_t, acc);
                   acc = 1u;
                 }
               } else {
@@ -348,11 +383,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 for (int pr = 0; pr < 3; ++pr)
 #pragma unroll
                   for (int k = 0; k < 4; ++k) {
-                    if (SPLIT && pr == 2) {  // the leading product, own accumulator
-                      umma_f16(d + BN, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc, acc_lead);
-                      acc_lead = 1u;
+                    if (SPLIT && pr < 2) {  // small products: the tile's own accumulator
+                      umma_f16(tsmall, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc_t,
+                               acc_small);
+                      acc_small = 1u;
                     } else {
-                      umma_f16(d, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc, acc);
+                      umma_f16(d, prs[pr][0] + 2 * k, prs[pr][1] + 2 * k, idesc_t, acc);
                       acc = 1u;
                     }
                   }
@@ -418,21 +454,28 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         tc_fence_after();
         const double cscale = first ? p.beta : 1.0;  // beta applies once per tile
         const bool need_old = !p.atomic_out && cscale != 0.0;
+        const bool last = c0 + p.kb_chunk >= kb1;   // SPLIT: add the small products now
         double* crow = p.C + roff;
-        const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * L::ACC);
+        const uint32_t lanes = (uint32_t)(q * 32) << 16;
+        const uint32_t tbase = tmem + lanes + (uint32_t)(b * L::ACC);
+        const uint32_t sbase = tmem + lanes + (uint32_t)L::SMALL;
         constexpr int NFULL = BN / 64;  // whole 32-column blocks per warp
 #pragma unroll 1
         for (int fb = 0; fb < NFULL; ++fb)
           epi_batch<32, SPLIT>(tbase + 32 * (2 * fb + h), colofs + 32 * fb, colsc + 32 * fb,
-                               row_ok, crow, ascale, cscale, need_old, p.atomic_out, BN);
+                               row_ok, crow, ascale, cscale, need_old, p.atomic_out,
+                               sbase + 32 * (2 * fb + h), last);
         if constexpr (BN % 64 != 0)  // BN = 96, 160, 224: the last block split 16 / 16
           epi_batch<16, SPLIT>(tbase + (BN - 32) + 16 * h, colofs + 32 * NFULL,
                                colsc + 32 * NFULL, row_ok, crow, ascale, cscale, need_old,
-                               p.atomic_out, BN);
+                               p.atomic_out, sbase + (BN - 32) + 16 * h, last);
         first = false;
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&tempty[b]);
+        if (lane == 0) {
+          mbar_arrive(&tempty[b]);
+          if (SPLIT && last) mbar_arrive(&sempty[0]);
+        }
       }
     }
   }
@@ -1007,7 +1050,12 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   int BN = 64;
   long long best = -1;
   for (int bn : kBN) {
-    if (split_acc && bn > 128) continue;  // four accumulators in 512 TMEM columns
+    if (split_acc && bn > 160) continue;  // three accumulators in 512 TMEM columns
+    // fused split formats hold hi and lo of both operands per stage: above 160 columns only
+    // two stages fit in shared memory, and the pipeline then stalls on TMA latency
+    // (measured on GB300: 160 columns and three stages issue 1450-1680 TFLOP/s on the
+    // ladder and ring shapes, 224 or 256 columns and two stages 1140-1510)
+    if (fused && bn > 160) continue;
     const long long tiles = ((M + BM - 1) / BM) * ((N + bn - 1) / bn);
     const long long slots = tiles >= sms_all ? (tiles + sms_all - 1) / sms_all * sms_all : tiles;
     const long long cost = slots * (bn + 48);
@@ -1033,6 +1081,19 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   splits = (nkb + kps - 1) / kps;
   a.mt = mt;
   a.nt = nt;
+  // raster group: a wave of W CTAs touches gm A row blocks (BM rows) and W / gm B row
+  // blocks (BN rows); gm = sqrt(W BN / BM) minimises their sum.  A narrow N (nt <= W / gm)
+  // keeps the N-fastest order (gm = 1): the CTAs sharing an A row block are then adjacent
+  // and each A block is read once per wave (measured on GB300: the ladder's 6 N tiles run
+  // 7-8 % faster this way than in groups of M-fastest tiles; the 12000 x 12000 ring GEMMs
+  // 12 % faster in groups than N-fastest).
+  {
+    const long long W = std::min<long long>(mt * nt * splits, sms_all);
+    long long gm = (long long)std::llround(std::sqrt((double)W * BN / BM));
+    gm = std::max(1LL, std::min(gm, mt));
+    if (nt * gm <= W) gm = 1;
+    a.gm = (int)gm;
+  }
   a.splits = splits;
   a.nkb_total = nkb;
   a.kb_per_split = kps;
@@ -1058,7 +1119,8 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
     switch (BN) {
       case 64: return launch<64, 2, true>(maps, a, st);
       case 96: return launch<96, 2, true>(maps, a, st);
-      default: return launch<128, 2, true>(maps, a, st);
+      case 128: return launch<128, 2, true>(maps, a, st);
+      default: return launch<160, 2, true>(maps, a, st);
     }
   }
   if (fused) {

@@ -24,9 +24,11 @@ def frob(a, b):
 
 @pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_FP8])
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (200, 70, 100), (37, 300, 513), (64, 180, 96),
-                                   (100, 210, 64), (150, 150, 64), (300, 820, 200)])
+                                   (100, 210, 64), (150, 150, 64), (300, 820, 200),
+                                   (3000, 2000, 64)])
 def test_gemm_exact_integers(cuda, fmt, M, N, K):
-    """N = 70, 150, 180, 210, 820 select the 96-, 160-, 192- and 224-column tiles."""
+    """N = 70, 150, 180, 210, 820 select the 96-, 160-, 192- and 224-column tiles (fused
+    formats stop at 160); 3000 x 2000 walks several raster groups, the last one partial."""
     g = torch.Generator(device=cuda).manual_seed(M + N + K)
     A = torch.randint(-3, 4, (M, K), generator=g, device=cuda).double()
     B = torch.randint(-3, 4, (N, K), generator=g, device=cuda).double()
