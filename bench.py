@@ -25,6 +25,7 @@ Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|referenc
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -363,7 +364,7 @@ def term_mode(args, dev):
                       "device_gb": torch.cuda.max_memory_allocated(dev) / 1e9}))
 
 
-def adjoint_mode(args, dev, directions=16):
+def adjoint_mode(args, dev):
     """Adjoint at no=20, nv=180 (seed 3, matched coupling): Lambda + gradient densities,
     backward/forward cost, central finite differences along random symmetric directions;
     the tape's sweeps on the engine ``--adjoint-sweep`` names."""
@@ -376,12 +377,13 @@ def adjoint_mode(args, dev, directions=16):
     fac = pg.SyntheticFactors(no, nv, seed, coupling="matched")
     H = pg.Hamiltonian.from_factors(fac, device=dev)
     w = pg.CCwfn(H)
-    e = w.solve_cc(1e-12, 1e-12, 100)
+    e = w.solve_cc(1e-12, 1e-12, 100, keep_tape=bool(args.keep_tape))
     fwd = float(np.mean(w.iter_times[1:]))
     torch.cuda.synchronize()
     t0 = time.time()
     adj = CCSDAdjoint(w, sweep=args.adjoint_sweep)
-    adj.solve_lambda(1e-12, 1e-12, 200)
+    t_tape = time.time() - t0
+    adj.solve_lambda(1e-12, 1e-12, 200, polish=bool(args.lambda_polish))
     gF, Gam = adj.gradient()
     torch.cuda.synchronize()
     t_back = time.time() - t0
@@ -390,8 +392,14 @@ def adjoint_mode(args, dev, directions=16):
     ERI = contract_f64("Qpr,Qqs->pqrs", B, B)
     F = H.F
     ident = float((gF * F).sum() + (Gam * ERI).sum()) - e
-    h, rows = 1e-5, []
-    for d in range(directions):
+    # fourth-order central differences, every point converged (|dE| < 1e-14, rms < 1e-13)
+    # from the unperturbed amplitudes: (8 (E(h) - E(-h)) - (E(2h) - E(-2h))) / 12h.  The
+    # directional derivatives along random unit directions of the n^4 space are small
+    # (1e-7 .. 1e-4), so h = 3e-2 keeps the rounding term (~1e-14 / h) far below 1e-6 of
+    # them; the h^4 truncation term was measured below 2e-8 relative against h = 1e-2.
+    h, rows = 3e-2, []
+    t1c, t2c = w.t1.clone(), w.t2.clone()
+    for d in range(args.fd_directions):
         g = torch.Generator(device=dev).manual_seed(100 + d)
         dF = torch.randn(n, n, dtype=torch.float64, device=dev, generator=g)
         dF = 0.5 * (dF + dF.T)
@@ -405,16 +413,24 @@ def adjoint_mode(args, dev, directions=16):
         dF /= nrm
         dE /= nrm
         an = float((gF * dF).sum() + (Gam * dE).sum())
-        es = []
-        for sg in (1.0, -1.0):
+        es = {}
+        for sg in (1.0, -1.0, 2.0, -2.0):
             wp = pg.CCwfn(pg.Hamiltonian.from_full(F + sg * h * dF, ERI + sg * h * dE, no))
-            es.append(wp.solve_cc(1e-12, 1e-12, 200))
+            wp.t1, wp.t2 = t1c, t2c
+            es[sg] = wp.solve_cc(1e-14, 1e-13, 200)
             del wp
-        fd = (es[0] - es[1]) / (2 * h)
+            gc.collect()            # a wave function is a reference cycle (self.contract)
+        fd = (8.0 * (es[1.0] - es[-1.0]) - (es[2.0] - es[-2.0])) / (12.0 * h)
         rows.append({"fd": fd, "adjoint": an, "abs": abs(fd - an), "rel": abs(fd - an) / abs(an)})
         del dE, dF
         torch.cuda.empty_cache()
-    line = {"mode": "adjoint", "sweep": args.adjoint_sweep,
+    stages = getattr(adj, "lambda_stages", [])
+    st_time = {k: float(sum(t for t, s_ in zip(adj.lambda_times, stages) if s_ == k))
+               for k in set(stages)}
+    line = {"mode": "adjoint", "sweep": args.adjoint_sweep, "lambda_polish": bool(args.lambda_polish),
+            "tape_from_last_forward_iteration": adj.tape_reused, "tape_s": t_tape,
+            "lambda_stages": {k: stages.count(k) for k in set(stages)},
+            "lambda_stage_s": st_time, "lambda_at_floor": getattr(adj, "lambda_at_floor", False),
             "config": {"no": no, "nv": nv, "seed": seed, "coupling": "matched"},
             "ecc": e, "forward_iter_s": fwd, "forward_niter": w.niter,
             "lambda_niter": adj.lambda_niter,
@@ -422,7 +438,9 @@ def adjoint_mode(args, dev, directions=16):
             "vjp_over_forward_iter": float(np.mean(adj.lambda_times[1:])) / fwd,
             "backward_s": t_back, "backward_over_forward_iter": t_back / fwd,
             "gradient_s": adj.timing_gradient, "energy_identity_err": ident,
-            "fd_max_abs": max(r["abs"] for r in rows), "fd_max_rel": max(r["rel"] for r in rows),
+            "fd_max_abs": max((r["abs"] for r in rows), default=None),
+            "fd_max_rel": max((r["rel"] for r in rows), default=None),
+            "fd_stencil": "4-point central, h=3e-2, points converged to |dE| < 1e-14",
             "fd": rows}
     print(json.dumps(line))
 
@@ -456,6 +474,12 @@ def main():
                     help="size of the CPU sample (default no=20, nv=180, seed 1)")
     ap.add_argument("--ref-budget", type=float, default=120.0,
                     help="reference arm: seconds of timed CPU iterations at most")
+    ap.add_argument("--fd-directions", type=int, default=16,
+                    help="adjoint mode: random directions of the finite-difference check")
+    ap.add_argument("--keep-tape", type=int, default=1, choices=[0, 1],
+                    help="adjoint mode: adopt the converging forward iteration's tape")
+    ap.add_argument("--lambda-polish", type=int, default=1, choices=[0, 1],
+                    help="adjoint mode, tensor-core sweeps: finish Lambda on the FP64 kernels")
     ap.add_argument("--term", default="nb,mnej->mbej")
     ap.add_argument("--term-fmt", default="bf16x3f", choices=["bf16", "bf16x3", "bf16x3f"])
     args = ap.parse_args()

@@ -19,6 +19,14 @@ extern "C" {
 /* ---- library ------------------------------------------------------------------------- */
 const char* pcg_last_error(void);
 int pcg_abi_version(void);
+/* Failure detection of the tensor-core kernels (no counterpart in the reference, whose only
+ * failure handling is input validation, pycc/exceptions.py:27-50): every device-side wait
+ * is bounded.  pcg_set_wait_limit_ns sets the bound (ns) passed to the kernels launched from
+ * then on (<= 0: the 4 s default; capped at 600 s) and returns the previous one.
+ * pcg_wait_probe launches a self-test that waits on an mbarrier nothing completes, with that
+ * bound, and sets *status (device int) to 4 when the wait expires. */
+long long pcg_set_wait_limit_ns(long long ns);
+int pcg_wait_probe(int* status, void* stream);
 /* number of kernels this library has launched since it was loaded */
 long long pcg_launch_count(void);
 /* compute capability of the current device as major*10+minor (103 on GB300) */
@@ -99,8 +107,9 @@ int pcg_dots_f64(const double* x, const double* const* ys, int k, long long n, d
  * instead of a caller-provided work buffer.  For host programs that own all device memory
  * (or must avoid cudaMalloc's implicit synchronisation) and so cannot hand the library
  * scratch.  The first call on a device looks the array's device address up
- * (cudaGetSymbolAddress); make it before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race.  k > 8 is rejected. */
+ * (cudaGetSymbolAddress); make it before any stream capture.  The address is cached for the
+ * process's life: do not use the library across a cudaDeviceReset of that device.  All calls
+ * share the array: calls that overlap on the GPU race.  k > 8 is rejected. */
 int pcg_dots_f64_noalloc(const double* x, const double* const* ys, int k, long long n,
                          double* out, void* stream);
 

@@ -24,6 +24,8 @@ SIGNATURES = {
     "pcg_launch_count": (C.c_longlong, []),
     "pcg_device_cc": (C.c_int, []),
     "pcg_stream_sync": (C.c_int, [_p]),
+    "pcg_set_wait_limit_ns": (C.c_longlong, [_i64]),
+    "pcg_wait_probe": (C.c_int, [_p, _p]),
     "pcg_contract_f64": (C.c_int, [C.c_int, _pi64, _pi64, _pi64, C.c_int, _pi64, _pi64, _pi64,
                                    C.c_int, _pi64, _pi64, _pi64, _d, _p, _p, _d, _p, _p]),
     "pcg_tau_f64": (C.c_int, [_p, _p, _i64, _i64, _d, _d, _p, _p]),
@@ -101,6 +103,12 @@ def call(name, *args):
         msg = lib.pcg_last_error().decode(errors="replace")
         raise EngineError("%s failed (%d): %s" % (name, rc, msg))
     return rc
+
+
+def set_wait_limit_ns(ns: int) -> int:
+    """Bound (ns) on any single device-side wait of the tensor-core kernels launched from now
+    on (<= 0 restores the 4 s default); returns the previous bound."""
+    return int(load().pcg_set_wait_limit_ns(int(ns)))
 
 
 def launch_count() -> int:

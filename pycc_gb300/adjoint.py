@@ -133,6 +133,9 @@ class CCSDAdjoint:
         self.sweep = sweep
         self.tc_min_flops = TC_MIN_FLOPS
         self._tc = None
+        self._tc_on = True        # a 'tc' sweep's contractions go to the tensor cores
+        from .tc import FMT_BF16X3S
+        self._tc_fmt = FMT_BF16X3S
         if sweep == 'tc':
             from .tc import TCEngine
             self._tc = TCEngine(w.device1, w.stream)
@@ -143,13 +146,23 @@ class CCSDAdjoint:
         for t in [H.F] + list(H.ERI.blocks.values()) + list(H.L.blocks.values()):
             self.leaves_H.add(_key(t))
         self.t1, self.t2 = w.t1, w.t2
-        tape = Tape()
+        last = getattr(w, "_last_tape", None)
+        self.tape_reused = (last is not None and w._tape_version is not None
+                            and w._tape_version == w._amps._version)
+        if self.tape_reused:
+            # the converging iteration of solve_cc(keep_tape=True) taped its residual
+            tape, self.r1, self.r2 = last
+        else:
+            tape = Tape()
         w._tape = tape
         try:
-            self.r1, self.r2 = w.residuals(H.F, self.t1, self.t2)
+            if not self.tape_reused:
+                self.r1, self.r2 = w.residuals(H.F, self.t1, self.t2)
             self.E = w.cc_energy_contractions(w.o, w.v, H.F, H.L, self.t1, self.t2)
         finally:
             w._tape = None
+        if self.tape_reused:
+            w._last_tape = w._tape_version = None     # the tape now carries the energy ops
         self.tape = tape
         self.grads = Grads()
         self.wrt_H = False
@@ -157,12 +170,13 @@ class CCSDAdjoint:
         self._scal = torch.zeros(4, dtype=torch.float64, device=H.F.device)
 
     # -- the sweeps' contractions ----------------------------------------------------------
-    def _mm(self, subs, A, B, out, alpha, beta):
-        """out = beta*out + alpha*einsum(subs, A, B): on the tensor cores for a 'tc' sweep and a
+    def _mm(self, subs, A, B, out, alpha, beta, fp64=False):
+        """out = beta*out + alpha*einsum(subs, A, B): on the FP64 kernel when ``fp64``, else on
+        the tensor cores for a 'tc' sweep and a
         GEMM-shaped contraction (an output index, none in both operands and the output,
         K >= 64) of at least ``tc_min_flops`` multiply-adds whose output offsets stay below
         2^31 (the tensor-core epilogue's column offsets are 32-bit), else on the FP64 kernel."""
-        if self._tc is not None:
+        if self._tc is not None and self._tc_on and not fp64:
             lhs, rhs = subs.replace(" ", "").split("->")
             la, lb = lhs.split(",")
             ext = dict(zip(la, A.shape))
@@ -173,10 +187,10 @@ class CCSDAdjoint:
             span = sum((e - 1) * st for e, st in zip(out.shape, out.stride()))
             if (rhs and not (set(la) & set(lb) & set(rhs)) and K >= 64
                     and M * N * K >= self.tc_min_flops and span < 2 ** 31):
-                from .tc import FMT_BF16X3S, Operand
+                from .tc import Operand
                 opA = Operand(la, (A, la), key=self._static_key(A))
                 opB = Operand(lb, (B, lb), key=self._static_key(B))
-                self._tc.contract(subs, opA, opB, out, alpha=alpha, beta=beta, fmt=FMT_BF16X3S)
+                self._tc.contract(subs, opA, opB, out, alpha=alpha, beta=beta, fmt=self._tc_fmt)
                 return
         contract_f64(subs, A, B, out=out, alpha=alpha, beta=beta, stream=self.stream)
 
@@ -375,19 +389,47 @@ class CCSDAdjoint:
                   _lib.i64s(out.stride()), _lib.stream_handle(self.stream))
         return out
 
+    STALL_RATIO = 0.8     # a 'tc' Lambda iteration above this fraction of the best rms stalls
+    STALL_ITERS = 2       # stalled iterations that end the tensor-core stage
+
     def solve_lambda(self, e_conv=1e-10, r_conv=1e-10, maxiter=100, max_diis=8, start_diis=1,
-                     callback=None):
-        """Jacobi + DIIS on J^T lambda = -dE/dt; returns (l1, l2)."""
+                     callback=None, polish=True):
+        """Jacobi + DIIS on J^T lambda = -dE/dt; returns (l1, l2).
+
+        With a 'tc' sweep the iterations start on the tensor cores.  Their split-BF16x3
+        products leave a rounding floor in the update norm (about 1e-7 relative); once the
+        norm stalls (``STALL_ITERS`` iterations above ``STALL_RATIO`` x its best) or the
+        criteria are met there, ``polish`` switches the sweeps to the FP64 kernels, which
+        converge the remaining digits.  Without ``polish`` the solve stops at the floor
+        (``self.lambda_at_floor``); ``gradient`` then removes the floor's effect on the
+        densities with one correction step (see there)."""
+        t0 = time.time()
+        self.lambda_times = []
+        self.lambda_stages = []
+        g1, g2 = self.dE_dt()
+        l1, l2, niter, at_floor = self._jacobi(g1, g2, e_conv, r_conv, maxiter, max_diis,
+                                               start_diis, callback, polish, "Lambda")
+        self.l1, self.l2 = l1, l2
+        self.lambda_niter = niter
+        self.lambda_at_floor = at_floor
+        self.timing_lambda = time.time() - t0
+        return l1, l2
+
+    def _jacobi(self, g1, g2, e_conv, r_conv, maxiter, max_diis, start_diis, callback, polish,
+                what, rel_floor=None):
+        """Solve (g + J^T x)_sym = 0 for x by Jacobi + DIIS on the sweep engine; returns
+        (x1, x2, iterations, stopped at the tensor cores' floor).  ``rel_floor``: stop once
+        the update norm is below this fraction of the first one."""
         w = self.w
         no, nv = w.no, w.nv
-        t0 = time.time()
-        g1, g2 = self.dE_dt()
+        tc_stage = self._tc is not None
+        self._tc_on = True
         lam = torch.zeros(no * nv + no * no * nv * nv, dtype=torch.float64, device=g1.device)
         l1 = lam[:no * nv].view(no, nv)
         l2 = lam[no * nv:].view(no, no, nv, nv)
         diis = DIIS(lam, max_diis, self.stream)
-        self.lambda_times = []
         pseudo_last, rms = 0.0, float("inf")
+        best, bad, first = float("inf"), 0, None
         for niter in range(1, maxiter + 1):
             ti = time.time()
             R1, R2 = self.jt_lambda(l1, l2, g1, g2)
@@ -403,31 +445,44 @@ class CCSDAdjoint:
             contract_f64("ijab,ijab->", l2, g2, out=pe, beta=1.0, stream=self.stream)
             vals = torch.stack([out.reshape(()), pe.reshape(())]).cpu().numpy()
             rms, pseudo = math.sqrt(max(float(vals[0]), 0.0)), float(vals[1])
+            self._check_tc()
+            first = rms if first is None else first
             self.lambda_times.append(time.time() - ti)
+            self.lambda_stages.append("tc" if tc_stage else "fp64")
             if callback is not None:
                 callback(niter, pseudo, pseudo - pseudo_last, rms)
-            if abs(pseudo - pseudo_last) < e_conv and rms < r_conv:
-                self.l1, self.l2 = l1, l2
-                self.lambda_niter = niter
-                self.timing_lambda = time.time() - t0
-                return l1, l2
+            done = abs(pseudo - pseudo_last) < e_conv and rms < r_conv
+            if rel_floor is not None and rms < rel_floor * first:
+                done = True
+            at_floor = False
+            if tc_stage:
+                bad = bad + 1 if rms > self.STALL_RATIO * best else 0
+                best = min(best, rms)
+                if polish and (done or bad >= self.STALL_ITERS):
+                    # the rest on the FP64 kernels, from the tensor-core iterate
+                    tc_stage = self._tc_on = False
+                    self.lambda_switch = niter
+                    if what == "Lambda":
+                        g1, g2 = self.dE_dt()
+                    diis = DIIS(lam, max_diis, self.stream)
+                    pseudo_last = pseudo
+                    continue
+                if not done and bad >= 2 * self.STALL_ITERS:
+                    at_floor = done = True          # the tensor cores' rounding floor
+            if done:
+                self._tc_on = True
+                self.lambda_rms = rms
+                return l1, l2, niter, at_floor
             pseudo_last = pseudo
             diis.add_error_vector(lam)
             if niter >= start_diis:
                 diis.extrapolate(lam)
-        raise ConvergenceError("Lambda", maxiter, pseudo - pseudo_last, rms)
+        self._tc_on = True
+        raise ConvergenceError(what, maxiter, pseudo - pseudo_last, rms)
 
     # -- gradient densities ---------------------------------------------------------------
-    def gradient(self, e_conv=1e-10, r_conv=1e-10, maxiter=100, l1=None, l2=None):
-        """dL/dF (nmo x nmo) and dL/d<pq|rs> (nmo^4) of the Lagrangian L = E + <l, r> at the
-        taped amplitudes: with the converged Lambda amplitudes (solved here when neither
-        (l1, l2) nor an earlier solve gives them) these are dE/dF and dE/d<pq|rs>."""
-        if l1 is None or l2 is None:
-            if not hasattr(self, "l1"):
-                self.solve_lambda(e_conv, r_conv, maxiter)
-            l1, l2 = self.l1, self.l2
-        t0 = time.time()
-        G = self.backward(gE=1.0, l1=l1, l2=l2, wrt_H=True)
+    def _densities(self, G):
+        """(dL/dF, dL/d<pq|rs>) from a sweep's leaf gradients (L blocks folded into ERI)."""
         w = self.w
         H = w.H
         no, nv, n = w.no, w.nv, w.nmo
@@ -444,6 +499,52 @@ class CCSDAdjoint:
                 accumulate(Gam[s[0], s[1], s[2], s[3]], g, 2.0, stream=self.stream)
                 accumulate(Gam[s[0], s[1], s[3], s[2]], g, -1.0, perm=(0, 1, 3, 2),
                            stream=self.stream)
+        return gF, Gam
+
+    def gradient(self, e_conv=1e-10, r_conv=1e-10, maxiter=100, l1=None, l2=None, refine=True):
+        """dL/dF (nmo x nmo) and dL/d<pq|rs> (nmo^4) of the Lagrangian L = E + <l, r> at the
+        taped amplitudes: with the converged Lambda amplitudes (solved here when neither
+        (l1, l2) nor an earlier solve gives them) these are dE/dF and dE/d<pq|rs>.
+
+        The density sweep runs on the FP64 kernels for every sweep engine: the tensor cores'
+        products (split-BF16x3 or x6, FP32 accumulation) leave 2-5e-6 of E in
+        E = <D, F> + <Gamma, ERI> at no=20, nv=180, where the FP64 sweep keeps it to 1e-14.
+
+        When Lambda stopped at the tensor cores' floor (``solve_lambda(polish=False)``) and
+        ``refine`` is set, the same FP64 sweep also yields the Lambda residual
+        R = dE/dt + J^T l at that Lambda (the sweep's gradient on t).  A correction d with
+        J^T d = -R is solved on the tensor cores to 1e-5 of R -- the floor times that is far
+        below FP64's own error -- and its densities <d, dr/dH> are added from one more
+        tensor-core sweep: they are ~1e-7 of the total, so its rounding does not show."""
+        if l1 is None or l2 is None:
+            if not hasattr(self, "l1"):
+                self.solve_lambda(e_conv, r_conv, maxiter)
+            l1, l2 = self.l1, self.l2
+            floor = getattr(self, "lambda_at_floor", False)
+        else:
+            floor = False
+        t0 = time.time()
+        tc_on = self._tc_on
+        self._tc_on = False
+        try:
+            G = self.backward(gE=1.0, l1=l1, l2=l2, wrt_H=True)
+        finally:
+            self._tc_on = tc_on
+        gF, Gam = self._densities(G)
+        self.lambda_refined = False
+        if floor and refine and self._tc is not None:
+            R1 = G.get(self.t1).clone()
+            R2 = self._sym_half(G.get(self.t2))
+            self.grads.clear()
+            d1, d2, _, _ = self._jacobi(R1, R2, 0.0, 0.0, 50, 8, 1, None, False,
+                                        "Lambda correction", rel_floor=1e-5)
+            G = self.backward(gE=0.0, l1=d1, l2=d2, wrt_H=True)
+            dF, dGam = self._densities(G)
+            gF += dF
+            Gam += dGam
+            self.l1 = l1 + d1
+            self.l2 = l2 + d2
+            self.lambda_refined = True
         torch.cuda.synchronize()
         self.timing_gradient = time.time() - t0
         self.grads.clear()
@@ -473,7 +574,7 @@ class CCSDEnergy(torch.autograd.Function):
         from .hamiltonian import Hamiltonian
         H = Hamiltonian.from_full(F.detach(), ERI.detach(), int(no))
         w = CCwfn(H, precision='DP')
-        e = w.solve_cc(e_conv, r_conv, 200)
+        e = w.solve_cc(e_conv, r_conv, 200, keep_tape=True)
         ctx.w = w
         ctx.conv = (e_conv, r_conv)
         return torch.tensor(e, dtype=torch.float64, device=F.device)

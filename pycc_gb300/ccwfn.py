@@ -131,6 +131,9 @@ class CCwfn:
         self.stream = None
         self._backend = ContractionBackend(self.device1, self.stream)
         self._tape = None         # set by pycc_gb300.adjoint while a residual is recorded
+        self._keep_tape = False   # solve_cc(keep_tape=True): tape every iteration's residual
+        self._last_tape = None    # (tape, r1, r2) of the last taped iteration
+        self._tape_version = None # amplitude version the kept tape belongs to
         self.contract = self._contract
         self._work = torch.empty(WORK_LEN, dtype=torch.float64, device=self.device1)
         self._scalars = torch.zeros(8, dtype=torch.float64, device=self.device1)
@@ -542,14 +545,25 @@ class CCwfn:
         o, v, F, L = self.o, self.v, self.H.F, self.H.L
         if self.precision in ('MIXED', 'SP'):
             self.mixed_engine().select_mode(self._last_rms)
-        r1, r2 = self.residuals(F, self.t1, self.t2)
+        keep = self._keep_tape and self.precision == 'DP'
+        if keep:               # the adjoint can adopt the last iteration's tape
+            from .adjoint import Tape
+            self._tape = Tape()
+        try:
+            r1, r2 = self.residuals(F, self.t1, self.t2)
+        finally:
+            tape, self._tape = self._tape, None
+        self._last_tape = (tape, r1, r2) if keep else None
         rms_t = self.update_amplitudes(r1, r2)
         e_t = self.cc_energy(o, v, F, L, self.t1, self.t2)
         del r1, r2
-        vals = torch.cat([e_t.reshape(1), rms_t.reshape(-1)]).cpu().numpy()
-        ecc, rms = float(vals[0]), math.sqrt(max(float(vals[1:].sum()), 0.0))
+        parts = [e_t.reshape(1), rms_t.reshape(-1)]
+        if self.precision in ('MIXED', 'SP'):   # the status words ride on the same read
+            parts.append(self.mixed_engine().tc.status.to(torch.float64))
+        vals = torch.cat(parts).cpu().numpy()
+        ecc, rms = float(vals[0]), math.sqrt(max(float(vals[1] + vals[2]), 0.0))
         if self.precision in ('MIXED', 'SP'):
-            self.mixed_engine().tc.check_status()
+            self.mixed_engine().tc.check_status(vals[3:])
         self.energies.append(ecc)
         self.iter_times.append(time.time() - t0)
         self.niter = niter
@@ -564,7 +578,7 @@ class CCwfn:
             diis.extrapolate(self._amps)       # in place
 
     def solve_cc(self, e_conv=1e-7, r_conv=1e-7, maxiter=100, max_diis=8, start_diis=1,
-                 callback=None):
+                 callback=None, keep_tape=False):
         """Jacobi + DIIS iteration to convergence; returns the correlation energy (float).
 
         Convergence: |dE| < e_conv and rms < r_conv (ccwfn.py:295).  In the MIXED / SP
@@ -573,8 +587,15 @@ class CCwfn:
         reported as the mean of the last four iterates (``self.converged_at_floor``).
         Raises :class:`ConvergenceError` if ``maxiter`` is exhausted and
         :class:`NumericalError` if the energy or the update norm turns NaN/Inf.
+
+        ``keep_tape`` (DP): every iteration records its residual on an adjoint tape and the
+        last one is kept, so that :class:`pycc_gb300.adjoint.CCSDAdjoint` adopts it instead
+        of evaluating the residual again at the converged amplitudes.  The taped residual is
+        the converging iteration's, at amplitudes one update (below ``r_conv``) away.
         """
         t_start = time.time()
+        self._keep_tape = bool(keep_tape)
+        self._tape_version = None
         self.e_conv, self.r_conv, self.maxiter = e_conv, r_conv, maxiter
         self.converged_at_floor = False
         diis = self.start_iterations(max_diis)
@@ -607,6 +628,11 @@ class CCwfn:
             if done:
                 self.ecc = ecc
                 self.timing["solve"] = time.time() - t_start
+                self._keep_tape = False
+                if self._last_tape is not None:
+                    # valid while the amplitudes stay as converged (torch's version counter
+                    # of the amplitude buffer records every later in-place change)
+                    self._tape_version = self._amps._version
                 if self.model == 'CCSD(T)':
                     from .triples import t_energy
                     et = t_energy(self)

@@ -6,8 +6,11 @@
 namespace pcg {
 static thread_local char g_err[512] = {0};
 static std::atomic<long long> g_launches{0};
+constexpr long long kDefaultWaitNs = 4000000000LL;
+static std::atomic<long long> g_wait_ns{kDefaultWaitNs};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long wait_limit_ns() { return (unsigned long long)g_wait_ns.load(); }
 
 void set_error(const char* fmt, ...) {
   va_list ap;
@@ -20,6 +23,14 @@ void set_error(const char* fmt, ...) {
 extern "C" const char* pcg_last_error(void) { return pcg::g_err; }
 
 extern "C" int pcg_abi_version(void) { return 2; }
+
+// Bound on any single device-side wait of the kernels launched from now on (ns); ns <= 0
+// restores the 4 s default, larger bounds are capped at 600 s.  Returns the previous bound.
+extern "C" long long pcg_set_wait_limit_ns(long long ns) {
+  if (ns <= 0) ns = pcg::kDefaultWaitNs;
+  if (ns > 600000000000LL) ns = 600000000000LL;
+  return pcg::g_wait_ns.exchange(ns);
+}
 
 // Kernels launched by this library since it was loaded (all threads, all streams).
 extern "C" long long pcg_launch_count(void) { return pcg::g_launches.load(); }

@@ -11,6 +11,9 @@ namespace pcg {
 void set_error(const char* fmt, ...);
 // Counts kernel launches issued by the library (read with pcg_launch_count).
 void note_launch();
+// Current bound (ns) on any single device-side wait of the tensor-core kernels
+// (pcg_set_wait_limit_ns; 4 s by default).  Passed to the kernels as an argument.
+unsigned long long wait_limit_ns();
 
 // Up to four sub-indices of one index group (M, N or K) of a contraction; each carries
 // its extent and its element stride in the two tensors that hold it.
@@ -82,6 +85,7 @@ enum DeviceStatus : int {
   kStatusTimeoutFull = 1,
   kStatusTimeoutEmpty = 2,
   kStatusTimeoutDone = 3,
+  kStatusTimeoutProbe = 4,  // pcg_wait_probe: the self-test's wait expired, as it should
 };
 
 }  // namespace pcg

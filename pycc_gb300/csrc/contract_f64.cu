@@ -163,12 +163,26 @@ __global__ void scale_strided_kernel(SubIdx m, SubIdx n, long long M, long long 
   }
 }
 
-// Outputs with a degenerate free dimension (matrix-vector shapes such as 'nf,mnef->me'):
-// one warp per output element, a warp-wide FP64 dot over K.  HBM-bound.
+// Stores one partial (or the whole) dot product of an output element: with K split across
+// blocks (blockIdx.y) the partials are atomic FP64 adds onto C, which the host scaled by
+// beta first.
+__device__ __forceinline__ void gemv_store(const F64Args& p, double* dst, double acc) {
+  const double v = p.alpha * acc;
+  if (p.atomic_out)
+    atomicAdd(dst, v);
+  else
+    *dst = (p.beta == 0.0) ? v : p.beta * *dst + v;
+}
+
+// Outputs with a degenerate free dimension (matrix-vector shapes such as 'nf,mnef->me', and
+// full dot products): one warp per output element and K slice (blockIdx.y), a warp-wide FP64
+// dot over the slice.  HBM-bound.
 __global__ void contract_gemv_kernel(const F64Args p) {
   const long long warps = ((long long)gridDim.x * blockDim.x) >> 5;
   const int lane = threadIdx.x & 31;
   const long long total = p.M * p.N;
+  const long long kbeg = (long long)blockIdx.y * p.k_per_split;
+  const long long kend = min(p.K, kbeg + p.k_per_split);
   for (long long o = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; o < total;
        o += warps) {
     const long long m = o / p.N, n = o % p.N;
@@ -178,51 +192,50 @@ __global__ void contract_gemv_kernel(const F64Args p) {
     double acc = 0.0;
     if (p.k.n == 1) {
       const long long sa = p.k.s0[0], sb = p.k.s1[0];
-      for (long long k = lane; k < p.K; k += 32) acc += p.A[am + k * sa] * p.B[bn + k * sb];
+      for (long long k = kbeg + lane; k < kend; k += 32) acc += p.A[am + k * sa] * p.B[bn + k * sb];
     } else {
-      for (long long k = lane; k < p.K; k += 32) {
+      for (long long k = kbeg + lane; k < kend; k += 32) {
         long long ka, kb;
         sub_offsets(p.k, k, ka, kb);
         acc += p.A[am + ka] * p.B[bn + kb];
       }
     }
     for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, s);
-    if (lane == 0) {
-      double* dst = p.C + cm + cn;
-      double v = p.alpha * acc;
-      *dst = (p.beta == 0.0) ? v : p.beta * *dst + v;
-    }
+    if (lane == 0) gemv_store(p, p.C + cm + cn, acc);
   }
 }
 
 // Matrix-vector shapes whose operand B is unit-stride along the output's innermost
 // sub-index: one thread per output, consecutive threads on consecutive outputs (coalesced
-// B reads); the K offsets are staged in shared memory once per block.
+// B reads); the K offsets are staged in shared memory once per block; blockIdx.y is the K
+// slice.
 __global__ void __launch_bounds__(256) contract_gemv_thread_kernel(const F64Args p) {
   __shared__ long long ka[256], kb[256];
   const long long o = (long long)blockIdx.x * 256 + threadIdx.x;
   const bool valid = o < p.M * p.N;
+  const long long kbeg = (long long)blockIdx.y * p.k_per_split;
+  const long long kend = min(p.K, kbeg + p.k_per_split);
   long long am = 0, cm = 0, bn = 0, cn = 0;
   if (valid) {
     sub_offsets(p.m, o / p.N, am, cm);
     sub_offsets(p.n, o % p.N, bn, cn);
   }
   double acc = 0.0;
-  for (long long k0 = 0; k0 < p.K; k0 += 256) {
+  for (long long k0 = kbeg; k0 < kend; k0 += 256) {
     __syncthreads();
     const long long k = k0 + threadIdx.x;
-    if (k < p.K) sub_offsets(p.k, k, ka[threadIdx.x], kb[threadIdx.x]);
+    if (k < kend) sub_offsets(p.k, k, ka[threadIdx.x], kb[threadIdx.x]);
     __syncthreads();
-    const int kn = (int)min((long long)256, p.K - k0);
+    const int kn = (int)min((long long)256, kend - k0);
     if (valid)
       for (int j = 0; j < kn; ++j) acc += p.A[am + ka[j]] * p.B[bn + kb[j]];
   }
-  if (valid) {
-    double* dst = p.C + cm + cn;
-    const double v = p.alpha * acc;
-    *dst = (p.beta == 0.0) ? v : p.beta * *dst + v;
-  }
+  if (valid) gemv_store(p, p.C + cm + cn, acc);
 }
+
+// K slices for a matrix-vector launch of `blocks` output blocks: enough blocks for about
+// eight per SM, each slice at least `kmin` long; beta is applied up front when split.
+long long gemv_splits(const F64Args& p, long long blocks, long long kmin);
 
 // Reorder sub-indices by decreasing |stride| in the operand (s0), unit stride innermost.
 void sort_by_operand_stride(SubIdx& d) {
@@ -262,6 +275,13 @@ bool fill_sub(SubIdx& d, int n, const long long* ext, const long long* s0, const
     d.s1[0] = 0;
   }
   return true;
+}
+
+long long gemv_splits(const F64Args& p, long long blocks, long long kmin) {
+  const long long want = 8LL * 152;
+  if (blocks >= want || p.K < 2 * kmin) return 1;
+  long long splits = std::min((want + blocks - 1) / blocks, p.K / kmin);
+  return std::max(1LL, std::min(splits, 65535LL));
 }
 
 int num_sms() {
@@ -319,7 +339,15 @@ extern "C" int pcg_contract_f64(int m_n, const long long* m_ext, const long long
     }
     if (q.n.s0[q.n.n - 1] == 1 && q.M * q.N >= 1024) {
       const long long blocks = (q.M * q.N + 255) / 256;
-      contract_gemv_thread_kernel<<<(unsigned)blocks, 256, 0, st>>>(q);
+      const long long splits = gemv_splits(q, blocks, 1024);
+      q.k_per_split = (q.K + splits - 1) / splits;
+      q.atomic_out = splits > 1;
+      if (q.atomic_out && beta != 1.0) {
+        scale_strided_kernel<<<(int)std::min<long long>((q.M * q.N + 255) / 256, 4096), 256, 0,
+                               st>>>(q.m, q.n, q.M, q.N, beta, C);
+        PCG_CHECK_LAUNCH("pcg_contract_f64/gemv_scale");
+      }
+      contract_gemv_thread_kernel<<<dim3((unsigned)blocks, (unsigned)splits), 256, 0, st>>>(q);
       PCG_CHECK_LAUNCH("pcg_contract_f64/gemv_thread");
       return 0;
     }
@@ -327,7 +355,15 @@ extern "C" int pcg_contract_f64(int m_n, const long long* m_ext, const long long
   if (p.M < 8 || p.N < 8) {
     long long warps = p.M * p.N;
     int blocks = (int)std::min<long long>((warps * 32 + 255) / 256, 152LL * 64);
-    contract_gemv_kernel<<<blocks, 256, 0, st>>>(p);
+    const long long splits = gemv_splits(p, blocks, 4096);
+    p.k_per_split = (p.K + splits - 1) / splits;
+    p.atomic_out = splits > 1;
+    if (p.atomic_out && beta != 1.0) {
+      scale_strided_kernel<<<(int)std::min<long long>((p.M * p.N + 255) / 256, 4096), 256, 0,
+                             st>>>(p.m, p.n, p.M, p.N, beta, C);
+      PCG_CHECK_LAUNCH("pcg_contract_f64/gemv_scale");
+    }
+    contract_gemv_kernel<<<dim3((unsigned)blocks, (unsigned)splits), 256, 0, st>>>(p);
     PCG_CHECK_LAUNCH("pcg_contract_f64/gemv");
     return 0;
   }

@@ -666,7 +666,10 @@ extern "C" int pcg_diis_error_f32(const double* x, const double* old, float* e,
 //   scratch, which every GPU that loads the library holds until the process exits.
 // * The array lives in device memory; host code only sees a stand-in symbol, so its device
 //   address is looked up once per device (cudaGetSymbolAddress) on the first call made
-//   with that device current.  Make that first call before any stream capture.
+//   with that device current.  Make that first call before any stream capture.  The
+//   address is cached for the life of the process: do not keep using the library across a
+//   cudaDeviceReset of that device (the reset unloads the module, and the array may come
+//   back at another address).
 // * Every call shares the array.  Each call writes every partial it later reads, so no
 //   clearing is needed, but calls that overlap on the GPU (different streams, or several
 //   host threads) race on it: serialise them.

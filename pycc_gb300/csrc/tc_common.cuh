@@ -11,7 +11,9 @@ constexpr int BM = 128;
 constexpr int KBYTES = 128;            // bytes of K per stage row (one 128B swizzle span)
 constexpr int NT = 192;          // grouped GEMM: warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int EPI_THREADS = 128;
-constexpr unsigned long long kWaitNs = 4000000000ull;  // 4 s bound on any single wait
+// Bound on any single device-side wait; the kernels take the bound as an argument (set per
+// launch from pcg_set_wait_limit_ns, 4 s by default).
+constexpr unsigned long long kWaitNs = 4000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -42,18 +44,19 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait on an mbarrier phase; false when the time bound expired.
-__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait on an mbarrier phase; false when limit_ns expired first.
+__device__ inline bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned long long limit_ns) {
   if (mbar_try(bar, parity)) return true;
   unsigned long long t0 = gtimer();
   for (;;) {
     for (int i = 0; i < 256; ++i)
       if (mbar_try(bar, parity)) return true;
-    if (gtimer() - t0 > kWaitNs) return false;
+    if (gtimer() - t0 > limit_ns) return false;
   }
 }
 // Bounded wait with nanosleep back-off, for threads off the critical issue path.
-__device__ inline bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) {
+__device__ inline bool mbar_wait_sleep(uint64_t* bar, uint32_t parity,
+                                       unsigned long long limit_ns) {
   if (mbar_try(bar, parity)) return true;
   unsigned long long t0 = gtimer();
   unsigned ns = 32;
@@ -62,7 +65,7 @@ __device__ inline bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) {
       if (mbar_try(bar, parity)) return true;
     __nanosleep(ns);
     if (ns < 256) ns <<= 1;
-    if (gtimer() - t0 > kWaitNs) return false;
+    if (gtimer() - t0 > limit_ns) return false;
   }
 }
 __device__ __forceinline__ void tma_load_2d(const CUtensorMap* tm, uint64_t* bar, void* dst, int x,

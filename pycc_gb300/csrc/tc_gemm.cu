@@ -67,6 +67,7 @@ struct Args {
   double* C;
   const float* a_scale;
   const float* b_scale;
+  unsigned long long wait_ns;  // bound on any single device-side wait
   const long long* col_map;   // optional per-column C offsets (replaces en)
   const double* col_scale;    // optional per-column multipliers
   int atomic_out;
@@ -277,7 +278,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           for (int pass = 0; pass < npass && !stop; ++pass) {
             for (int kb = c0; kb < c1; ++kb, ++it) {
               const int s = it % S;
-              if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1)) {
+              if (it >= S && !mbar_wait(&empty[s], ((it / S) - 1) & 1, p.wait_ns)) {
                 atomicExch(p.status, kStatusTimeoutEmpty);
                 *abort_flag = 1;
               }
@@ -299,7 +300,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       }
       if (stop) {
         // let the copies already in flight land before the CTA releases its shared memory
-        for (int j = max(0, it - S); j < it; ++j) mbar_wait(&full[j % S], (j / S) & 1);
+        for (int j = max(0, it - S); j < it; ++j)
+          mbar_wait(&full[j % S], (j / S) & 1, p.wait_ns);
       }
     }
     __syncwarp();
@@ -319,7 +321,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
         uint32_t acc_small = 0u;
         if (SPLIT && tl >= 1) {  // the previous tile's small-product sum has been read
-          if (!mbar_wait(&sempty[0], (tl - 1) & 1)) {
+          if (!mbar_wait(&sempty[0], (tl - 1) & 1, p.wait_ns)) {
             atomicExch(p.status, kStatusTimeoutEmpty);
             *abort_flag = 1;
           }
@@ -337,7 +339,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         for (int c0 = kb0; c0 < kb1 && !stop; c0 += p.kb_chunk, ++u) {
           const int c1 = min(c0 + p.kb_chunk, kb1);
           const int b = u & 1;
-          if (u >= 2 && !mbar_wait(&tempty[b], ((u >> 1) - 1) & 1)) {
+          if (u >= 2 && !mbar_wait(&tempty[b], ((u >> 1) - 1) & 1, p.wait_ns)) {
             atomicExch(p.status, kStatusTimeoutEmpty);
             *abort_flag = 1;
           }
@@ -352,7 +354,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           for (int pass = 0; pass < npass && !stop; ++pass) {
             for (int kb = c0; kb < c1; ++kb, ++it) {
               const int s = it % S;
-              if (!mbar_wait(&full[s], (it / S) & 1)) {
+              if (!mbar_wait(&full[s], (it / S) & 1, p.wait_ns)) {
                 atomicExch(p.status, kStatusTimeoutFull);
                 *abort_flag = 1;
               }
@@ -400,7 +402,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
       }
       umma_commit(mdone);
-      mbar_wait(mdone, 0);  // every MMA of this CTA has retired before TMEM is released
+      mbar_wait(mdone, 0, p.wait_ns);  // every MMA of this CTA retired before TMEM is released
     }
     __syncwarp();
   } else {
@@ -439,7 +441,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         // one lane polls (with back-off), the warp follows
         int okw = 1;
         if (lane == 0) {
-          okw = mbar_wait_sleep(&tfull[b], (u >> 1) & 1) ? 1 : 0;
+          okw = mbar_wait_sleep(&tfull[b], (u >> 1) & 1, p.wait_ns) ? 1 : 0;
           if (!okw) {
             atomicExch(p.status, kStatusTimeoutDone);
             *abort_flag = 1;
@@ -1040,6 +1042,7 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.col_map = col_map;
   a.col_scale = col_scale;
   a.status = status;
+  a.wait_ns = wait_limit_ns();
   // Tile width: the least SM time, counting whole waves of the persistent grid (a launch
   // with fewer tiles than SMs is split along K instead) and weighting each tile by its
   // columns plus its fixed A-operand share.

@@ -41,6 +41,7 @@ struct GArgs {
   long long mt, nt;
   float* C;
   int* status;
+  unsigned long long wait_ns;  // bound on any single device-side wait
 };
 
 template <int BN>
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 1)
           const CUtensorMap* tb = &maps.b[g.bmap[s]];
           for (int kb = 0; kb < g.nkb[s]; ++kb, ++it) {
             const int st = it % S;
-            if (it >= S && !mbar_wait(&empty[st], ((it / S) - 1) & 1)) {
+            if (it >= S && !mbar_wait(&empty[st], ((it / S) - 1) & 1, p.wait_ns)) {
               atomicExch(p.status, kStatusTimeoutEmpty);
               *abort_flag = 1;
             }
@@ -131,7 +132,8 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 1)
         }
       }
       if (stop)
-        for (int j = max(0, it - S); j < it; ++j) mbar_wait(&full[j % S], (j / S) & 1);
+        for (int j = max(0, it - S); j < it; ++j)
+          mbar_wait(&full[j % S], (j / S) & 1, p.wait_ns);
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -143,7 +145,7 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 1)
       for (long long u = blockIdx.x; u < nunits && !stop; u += gridDim.x, ++ui) {
         const GroupDesc& g = p.groups[u / per];
         const int b = ui & 1;
-        if (ui >= 2 && !mbar_wait(&tempty[b], ((ui >> 1) - 1) & 1)) {
+        if (ui >= 2 && !mbar_wait(&tempty[b], ((ui >> 1) - 1) & 1, p.wait_ns)) {
           atomicExch(p.status, kStatusTimeoutEmpty);
           *abort_flag = 1;
         }
@@ -154,7 +156,7 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 1)
         for (int s = 0; s < g.nseg && !stop; ++s) {
           for (int kb = 0; kb < g.nkb[s]; ++kb, ++it) {
             const int st = it % S;
-            if (!mbar_wait(&full[st], (it / S) & 1)) {
+            if (!mbar_wait(&full[st], (it / S) & 1, p.wait_ns)) {
               atomicExch(p.status, kStatusTimeoutFull);
               *abort_flag = 1;
             }
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 1)
         umma_commit(&tfull[b]);
       }
       umma_commit(mdone);
-      mbar_wait(mdone, 0);
+      mbar_wait(mdone, 0, p.wait_ns);
     }
     __syncwarp();
   } else {
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(GROUPED_THREADS, 1)
       const int b = ui & 1;
       int okw = 1;
       if (lane == 0) {
-        okw = mbar_wait_sleep(&tfull[b], (ui >> 1) & 1) ? 1 : 0;
+        okw = mbar_wait_sleep(&tfull[b], (ui >> 1) & 1, p.wait_ns) ? 1 : 0;
         if (!okw) {
           atomicExch(p.status, kStatusTimeoutDone);
           *abort_flag = 1;
@@ -301,6 +303,7 @@ extern "C" int pcg_tc_grouped_gemm(int na, const void* const* a_ptr, const long 
   a.mt = (M + BM - 1) / BM;
   a.C = C;
   a.status = status;
+  a.wait_ns = wait_limit_ns();
   cudaStream_t st = (cudaStream_t)stream;
   switch (BN) {
     case 64: return glaunch<64>(maps, a, st);

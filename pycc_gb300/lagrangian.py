@@ -94,10 +94,13 @@ class cclambda:
         self.l1 = _combine(2.0, ccwfn.t1, 0.0, None, st)
         self.l2 = _combine(4.0, ccwfn.t2, -2.0, (0, 1, 3, 2), st)
 
-    def solve_lambda(self, e_conv=1e-7, r_conv=1e-7, maxiter=100, max_diis=8, start_diis=1):
-        """Solve the Lambda equations; returns the pseudo-energy (float)."""
+    def solve_lambda(self, e_conv=1e-7, r_conv=1e-7, maxiter=100, max_diis=8, start_diis=1,
+                     polish=True):
+        """Solve the Lambda equations; returns the pseudo-energy (float).  ``polish``: see
+        :meth:`CCSDAdjoint.solve_lambda` (tensor-core sweeps only)."""
         w = self.ccwfn
-        l1, l2 = self.hbar.adjoint.solve_lambda(e_conv, r_conv, maxiter, max_diis, start_diis)
+        l1, l2 = self.hbar.adjoint.solve_lambda(e_conv, r_conv, maxiter, max_diis, start_diis,
+                                                polish=polish)
         self.l1 = l1.clone()
         self.l2 = _combine(2.0, l2, 0.0, None, w.stream)
         self.pseudo = self.pseudoenergy(w.o, w.v, w.H.ERI, self.l2)

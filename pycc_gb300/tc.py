@@ -298,7 +298,16 @@ class TCEngine:
             self.cache[key] = p
         return p
 
-    def check_status(self):
-        s = self.status.cpu()
-        if int(s.abs().sum()) != 0:
-            raise _lib.EngineError("tensor-core kernel reported a wait timeout (status %s)" % s.tolist())
+    STATUS_TEXT = {1: "a stage's TMA data never arrived", 2: "a stage or accumulator was "
+                   "never released", 3: "an accumulator was never completed",
+                   4: "the self-test's wait expired"}
+
+    def check_status(self, values=None):
+        """Raise EngineError when a kernel recorded an expired device-side wait.  ``values``:
+        the status words already read to the host (read here otherwise)."""
+        s = [int(x) for x in (self.status.cpu().tolist() if values is None else values)]
+        if any(s):
+            what = "; ".join(sorted({self.STATUS_TEXT.get(abs(x), "code %d" % x)
+                                     for x in s if x}))
+            raise _lib.EngineError("tensor-core kernel reported an expired wait (%s; status %s)"
+                                   % (what, s))

@@ -206,3 +206,26 @@ def test_degenerate_sizes(model, no, nv, sweep):
     lhs = float((l1 * dr1).sum() + (l2 * dr2).sum())
     rhs = float((G.get(adj.t1) * x1).sum() + (G.get(adj.t2) * x2).sum())
     assert abs(lhs - rhs) <= 1e-11 * max(1.0, abs(lhs))
+
+
+def test_adjoint_adopts_the_last_forward_tape(model, ham_o5v19, golden_o5v19):
+    """solve_cc(keep_tape=True): the adjoint adopts the converging iteration's taped
+    residual instead of evaluating it again; Lambda and the densities still match the
+    reference's.  Any later change of the amplitudes makes the adjoint record afresh."""
+    g = golden_o5v19
+    w = wavefunction(ham_o5v19)
+    w.solve_cc(1e-12, 1e-12, keep_tape=True)
+    n0 = len(model.calls)
+    adj = CCSDAdjoint(w)
+    assert adj.tape_reused
+    assert "pcg_symmetrize_f64" not in model.calls[n0:]        # no residual evaluated
+    lam = pg.cclambda(w, pg.cchbar(w))                        # the tape is used once
+    assert not lam.hbar.adjoint.tape_reused
+    adj.solve_lambda(1e-12, 1e-12, 200)
+    gF, Gam = adj.gradient()
+    assert (0.5 * (gF + gF.T) - 0.5 * (torch.from_numpy(g["D"]) + torch.from_numpy(g["D"]).T)
+            ).abs().max().item() < 1e-9
+    assert (symmetrize8(Gam) - symmetrize8(torch.from_numpy(g["Gamma"]))).abs().max().item() < 1e-9
+    w.solve_cc(1e-12, 1e-12, keep_tape=True)
+    w.t1[0, 0] += 1e-3
+    assert not CCSDAdjoint(w).tape_reused

@@ -17,7 +17,8 @@ pytestmark = pytest.mark.skipif(torch.cuda.is_available(),
 
 # entry points without device pointers, or whose job is a CUDA call
 PLUMBING = {"pcg_last_error", "pcg_abi_version", "pcg_launch_count", "pcg_device_cc",
-            "pcg_stream_sync", "pcg_tc_group_desc_size", "pcg_triples_part_len"}
+            "pcg_stream_sync", "pcg_tc_group_desc_size", "pcg_triples_part_len",
+            "pcg_set_wait_limit_ns"}
 # argument values of the "plausible sizes, null pointers" call, by ctypes type
 DEFAULTS = {C.c_int: 1, C.c_longlong: 4, C.c_double: 1.0}
 

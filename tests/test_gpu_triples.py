@@ -1,7 +1,8 @@
 """(T) correction on the GPU against the reference's energies and the CPU oracle.
 
 Tolerances: FP64 path 1e-11 Eh (absolute) against t_tjl / t_vikings; the BF16 tensor-core
-path within 2e-3 relative of the FP64 value; the grouped GEMM is exact on integer data.
+path within 1e-5 Eh of the reference at no=5, nv=19 and 1e-6 Eh of the FP64 path at no=10,
+nv=80 (2e-3 relative on the small ragged cases); the grouped GEMM is exact on integer data.
 """
 import ctypes as C
 
@@ -38,7 +39,10 @@ def test_fp64_triples_golden_o5v19(w1, golden_o5v19):
 def test_tc_triples_golden_o5v19(w1, golden_o5v19):
     et = t_energy_tc(w1, batch=7)
     ref = float(golden_o5v19["et_tjl"])
-    assert abs(et - ref) < 2e-3 * abs(ref), (et, ref)
+    # BF16 operands: at this size few terms average the rounding out (measured 6.0e-6 Eh,
+    # 2e-4 relative; 6.5e-7 Eh at no=10, nv=80 and 8e-8 Eh at no=30, nv=240)
+    print("(T) o5v19: tc %.12f reference %.12f diff %.2e" % (et, ref, et - ref))
+    assert abs(et - ref) < 1e-5, (et, ref)
 
 
 @pytest.mark.parametrize("no,nv", [(3, 17), (6, 23)])
@@ -106,3 +110,17 @@ def test_grouped_gemm_exact(cuda, layout):
     assert torch.equal(out[0].double(), ref0)
     assert torch.equal(out[1].double(), ref1)
     assert int(st.abs().sum()) == 0
+
+
+def test_tc_triples_mid_size_vs_fp64(cuda):
+    """The tensor-core (T) (BF16 operands, FP32 accumulation, FP64 energy sum) against the
+    FP64 (T) at no=10, nv=80 (MP2 doubles, small random singles): within 1e-6 Eh, the
+    accuracy bar of the mixed-precision CCSD energy (measured: 6.5e-7 Eh, 1.8e-5 relative)."""
+    fac = pg.SyntheticFactors(10, 80, seed=4, coupling="matched")
+    w = pg.CCwfn(pg.Hamiltonian.from_factors(fac, device=cuda))
+    g = torch.Generator(device=cuda).manual_seed(10)
+    w.t1 = 0.01 * torch.randn(10, 80, dtype=torch.float64, device=cuda, generator=g)
+    e64 = t_energy_fp64(w)
+    etc = t_energy_tc(w, batch=32)
+    print("(T) no=10 nv=80: fp64 %.12f tc %.12f diff %.2e" % (e64, etc, etc - e64))
+    assert abs(etc - e64) < 1e-6

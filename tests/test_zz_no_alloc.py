@@ -3,9 +3,9 @@
 It exists for host programs that cannot give the library device scratch (they own all
 device memory, or must avoid cudaMalloc's implicit synchronisation): its partial sums live
 in a fixed array inside the library.  Checked here through the C ABI against the regular
-pcg_dots_f64 (caller-provided work buffer) on two calls in a row, with different inputs
-and vector counts, so the second call runs on the array the first one left behind.  This
-file is collected last.
+pcg_dots_f64 (caller-provided work buffer) and, independently of both, against torch's FP64
+dot products, on two calls in a row, with different inputs and vector counts, so the second
+call runs on the array the first one left behind.  This file is collected last.
 """
 import ctypes as C
 
@@ -45,6 +45,10 @@ def test_noalloc_matches_regular_two_calls(cuda):
         _dots_noalloc(lib, x, ys, got, st)
         torch.cuda.synchronize()
         assert torch.allclose(got, ref, rtol=RTOL, atol=RTOL * ref.abs().max().item()), (k, got, ref)
+        # an independent FP64 reference: torch's dot products of the same vectors
+        tdot = torch.stack([torch.dot(x, y) for y in ys])
+        scale = max(float(torch.linalg.norm(x)) * max(float(torch.linalg.norm(y)) for y in ys), 1.0)
+        assert (got - tdot).abs().max().item() < RTOL * scale, (k, got, tdot)
 
 
 def test_noalloc_rejects_too_many_vectors(cuda):
