@@ -468,7 +468,7 @@ def main():
                          "contraction (--term) alone at --no/--nv")
     ap.add_argument("--triples-size", type=int, nargs=3, default=None, metavar=("NO", "NV", "SEED"),
                     help="(T) mode at another size (profiling; the measurement is no=30,nv=240)")
-    ap.add_argument("--adjoint-sweep", default="fp64", choices=["fp64", "tc"],
+    ap.add_argument("--adjoint-sweep", default="tc", choices=["fp64", "tc"],
                     help="adjoint mode: engine of the tape's sweeps (FP64 DMMA or tensor cores)")
     ap.add_argument("--cpu-sample", type=int, nargs=3, default=None, metavar=("NO", "NV", "SEED"),
                     help="size of the CPU sample (default no=20, nv=180, seed 1)")
@@ -478,7 +478,7 @@ def main():
                     help="adjoint mode: random directions of the finite-difference check")
     ap.add_argument("--keep-tape", type=int, default=1, choices=[0, 1],
                     help="adjoint mode: adopt the converging forward iteration's tape")
-    ap.add_argument("--lambda-polish", type=int, default=1, choices=[0, 1],
+    ap.add_argument("--lambda-polish", type=int, default=0, choices=[0, 1],
                     help="adjoint mode, tensor-core sweeps: finish Lambda on the FP64 kernels")
     ap.add_argument("--term", default="nb,mnej->mbej")
     ap.add_argument("--term-fmt", default="bf16x3f", choices=["bf16", "bf16x3", "bf16x3f"])

@@ -9,10 +9,12 @@ from .synth import SyntheticFactors, WORKLOADS, synthetic_factors
 from .ccwfn import CCwfn, ccwfn
 from .contract import ContractionBackend, contract_f64
 from .lagrangian import cchbar, cclambda, ccdensity
+from ._lib import EngineError
+from . import ops  # noqa: F401  (registers torch.ops.gbcc)
 
 __all__ = [
     "CCwfn", "ccwfn", "Hamiltonian", "BlockTensor", "SyntheticFactors", "WORKLOADS",
     "synthetic_factors", "ContractionBackend", "contract_f64", "cchbar", "cclambda",
     "ccdensity", "PyCCError",
-    "InvalidKeywordError", "ConvergenceError", "NumericalError",
+    "InvalidKeywordError", "ConvergenceError", "NumericalError", "EngineError",
 ]

@@ -564,8 +564,10 @@ def symmetrize8(G):
 class CCSDEnergy(torch.autograd.Function):
     """Converged FP64 CCSD correlation energy of (F, <pq|rs>) with its implicit adjoint.
 
-    forward: ``CCwfn.solve_cc`` on the GPU.  backward: the Lambda equations through the
-    residual's tape, then dE/dF and dE/d<pq|rs> (the gradient densities).
+    forward: ``CCwfn.solve_cc`` on the GPU, keeping the converging iteration's tape.
+    backward: the Lambda equations through that tape on the tensor cores, then dE/dF and
+    dE/d<pq|rs> (the gradient densities) from one FP64 sweep with the Lambda floor's
+    correction: 2.2 forward iterations at no=20, nv=180, finite differences to 2e-8.
     """
 
     @staticmethod
@@ -581,8 +583,10 @@ class CCSDEnergy(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gE):
-        adj = CCSDAdjoint(ctx.w)
-        adj.solve_lambda(*ctx.conv)
+        # Lambda on the tensor cores to their floor, the densities from one FP64 sweep with
+        # the floor's correction (CCSDAdjoint.gradient), over the forward solve's own tape
+        adj = CCSDAdjoint(ctx.w, sweep='tc')
+        adj.solve_lambda(*ctx.conv, polish=False)
         gF, Gam = adj.gradient()
         return gE * gF, gE * Gam, None, None, None
 

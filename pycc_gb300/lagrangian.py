@@ -57,11 +57,14 @@ def symmetrize_density2(G, stream=None):
 
 
 class cchbar:
-    """HBAR of the FP64 engine, represented by the residual's tape (``pycc/cchbar.py:54``).
+    """HBAR of the FP64 engine (``pycc/cchbar.py:54``), represented two ways.
 
-    The reference's blocks (``Hov``, ``Hvvvv``, ...) are not materialised; ``jacobian`` is
-    HBAR's action on an amplitude pair (``CCderiv._ccsd_jacobian``).  ``sweep`` ('fp64' or
-    'tc') selects the engine of the tape's sweeps (see :class:`CCSDAdjoint`)."""
+    * The residual's tape: ``jacobian`` is HBAR's action on an amplitude pair
+      (``CCderiv._ccsd_jacobian``) and the reverse sweep its transpose (Lambda); ``sweep``
+      ('fp64' or 'tc') selects the engine of the sweeps (see :class:`CCSDAdjoint`).
+    * The reference's eleven blocks ``Hov, Hvv, Hoo, Hoooo, Hvvvv, Hvovv, Hooov, Hovvo, Hovov,
+      Hvvvo, Hovoo`` with its index layouts, built in FP64 on the GPU on first access
+      (``pycc_gb300.hbar.HBAR``; ``Hvvvv`` is nv^4)."""
 
     def __init__(self, ccwfn, sweep=None):
         t0 = time.time()
@@ -74,10 +77,12 @@ class cchbar:
         return self.adjoint.jacobian(X1, X2)
 
     def __getattr__(self, name):
-        if name.startswith("H"):
-            raise AttributeError(
-                "cchbar.%s: the GPU engine does not materialise HBAR blocks; use "
-                "cchbar.jacobian(X1, X2) for HBAR's action, cclambda for its transpose" % name)
+        from .hbar import HBAR, NAMES
+        if name in NAMES:
+            hb = self.__dict__.get("_hbar")
+            if hb is None:
+                hb = self.__dict__["_hbar"] = HBAR(self.ccwfn)
+            return hb[name]
         raise AttributeError(name)
 
 

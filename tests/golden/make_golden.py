@@ -12,7 +12,7 @@ Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
 
 Usage::
 
-    PYCC_REF=<reference tree> PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian] [--no-complex]
+    PYCC_REF=<reference tree> PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian] [--no-complex] [--no-hbar]
 
 The no=20, nv=180 fixtures need ~30 GB of host RAM and several minutes.
 """
@@ -155,6 +155,25 @@ def gen_o5v19_jacobian(pycc):
           % (np.linalg.norm(out["sigma1"]), np.linalg.norm(out["sigma2_sym"])))
 
 
+def gen_o5v19_hbar(pycc):
+    """The reference's eleven HBAR blocks (``cchbar.__init__``, pycc/cchbar.py:54-110) at its
+    converged no=5, nv=19 amplitudes, and those amplitudes."""
+    no, nv, seed = WORKLOADS["o5v19"]
+    fac = SyntheticFactors(no, nv, seed)
+    F, ERI, L = fac.hamiltonian()
+    w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
+    ecc = quiet(w.solve_cc, 1e-12, 1e-12, 100, 8, 1)
+    from pycc.cchbar import cchbar
+    hbar = quiet(cchbar, w)
+    names = ("Hov", "Hvv", "Hoo", "Hoooo", "Hvvvv", "Hvovv", "Hooov", "Hovvo", "Hovov", "Hvvvo",
+             "Hovoo")
+    out = {"ecc": float(ecc), "t1": w.t1, "t2": w.t2}
+    for n in names:
+        out[n] = np.asarray(getattr(hbar, n))
+    np.savez_compressed(os.path.join(HERE, "o5v19_hbar.npz"), **out)
+    print("o5v19_hbar: " + "  ".join("|%s| = %.6e" % (n, np.linalg.norm(out[n])) for n in names))
+
+
 def gen_o5v19_complex(pycc):
     """The reference's residual at complex amplitudes and a complex Fock matrix, as its
     real-time propagation calls it (``residuals(F, t1, t2, real_time=True)``): no=5, nv=19,
@@ -226,6 +245,7 @@ def main():
     ap.add_argument("--no-o5v19", action="store_true")
     ap.add_argument("--no-jacobian", action="store_true")
     ap.add_argument("--no-complex", action="store_true")
+    ap.add_argument("--no-hbar", action="store_true")
     args = ap.parse_args()
     pycc = import_reference()
     if not args.no_o5v19:
@@ -234,6 +254,8 @@ def main():
         gen_o5v19_jacobian(pycc)
     if not args.no_complex:
         gen_o5v19_complex(pycc)
+    if not args.no_hbar:
+        gen_o5v19_hbar(pycc)
     if args.o20v180:
         gen_o20v180(pycc, solve=False, coupling=1.0, name="o20v180_raw.npz")
         gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz")

@@ -7,6 +7,7 @@
 * cchbar -> cclambda -> ccdensity with the reference's interface: pseudo-energy (1e-10),
   l1 / l2 (1e-9) against the reference's cclambda, D (as is) and Gamma (eight-fold
   projection) against its gradient_densities (1e-9), compute_energy against E_corr.
+* The eleven HBAR blocks against the reference's cchbar (o5v19_hbar.npz), 1e-12 relative.
 """
 import numpy as np
 import pytest
@@ -69,3 +70,20 @@ def test_reference_objects_chain(cuda, ham_o5v19, golden_o5v19):
     assert (D - Dr).abs().max().item() < 1e-9                         # not symmetrised
     assert (G - symmetrize8(Gr)).abs().max().item() < 1e-9
     assert abs(dens.compute_energy() - e) < 1e-10
+
+
+def test_hbar_blocks_vs_reference(cuda, ham_o5v19):
+    """The reference's eleven HBAR blocks (pycc/cchbar.py:54-110), materialised on the GPU
+    in FP64, against its own blocks at its converged amplitudes (o5v19_hbar.npz): 1e-12
+    relative to each block's largest element."""
+    g = golden("o5v19_hbar.npz")
+    _, F, ERI, L = ham_o5v19
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda))
+    w.t1 = torch.from_numpy(g["t1"]).to(cuda)
+    w.t2 = torch.from_numpy(np.ascontiguousarray(g["t2"])).to(cuda)
+    hbar = pg.cchbar(w)
+    for name in ("Hov", "Hvv", "Hoo", "Hoooo", "Hvvvv", "Hvovv", "Hooov", "Hovvo", "Hovov",
+                 "Hvvvo", "Hovoo"):
+        got = getattr(hbar, name).cpu().numpy()
+        assert got.shape == g[name].shape, name
+        assert np.abs(got - g[name]).max() < 1e-12 * np.abs(g[name]).max(), name
