@@ -445,6 +445,57 @@ def adjoint_mode(args, dev):
     print(json.dumps(line))
 
 
+def fp64cfg2_mode(args, dev):
+    """Plain FP64 RHF-CCSD on the GPU at no=20, nv=180 (seed 1, matched coupling), converged
+    to 1e-10: s/iter, TFLOP/s, the fraction of the FP64 peak (cuBLAS DGEMM measured in the
+    same run, and the nominal 1.25 TFLOP/s), the energy error against the reference's own
+    converged energy (tests/golden/o20v180.npz), and the reference's CPU iteration on the
+    host cores at the same size."""
+    import numpy as np
+    import torch
+    import pycc_gb300 as pg
+    no, nv, seed = 20, 180, 1
+    fac = pg.SyntheticFactors(no, nv, seed, coupling="matched")
+    H = pg.Hamiltonian.from_factors(fac, device=dev)
+    w = pg.CCwfn(H)
+    t0 = time.time()
+    e = w.solve_cc(1e-10, 1e-10, args.fp64_maxiter)
+    torch.cuda.synchronize()
+    solve_s = time.time() - t0
+    s_iter = float(np.mean(w.iter_times[1:]))
+    tf = f_iter(no, nv) / s_iter / 1e12
+    # cuBLAS FP64 GEMM on the same GPU: the measured FP64 denominator
+    a = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+    b = torch.randn(8192, 8192, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(3):
+        torch.matmul(a, b)
+    e1.record()
+    torch.cuda.synchronize()
+    dgemm = 3 * 2 * 8192.0 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    del a, b
+    ref = None
+    gpath = os.path.join(ROOT, "tests", "golden", "o20v180.npz")
+    if os.path.exists(gpath):
+        ref = float(np.load(gpath)["ecc"])
+    cpu = None
+    if not args.no_cpu_baseline:
+        res = cpu_reference_iteration(2, 1, 30.0, (no, nv, seed))
+        cpu = {"s_per_iter": res["s_per_iter"], "tflops": res["tflops"], "kind": res["kind"],
+               "cores": res["cores"], "host": res["host"], "steps": res["steps"]}
+    print(json.dumps({"mode": "fp64cfg2", "config": {"no": no, "nv": nv, "seed": seed,
+                                                     "coupling": "matched"},
+                      "ecc": e, "niter": w.niter, "solve_s": solve_s, "s_per_iter": s_iter,
+                      "tflops": tf, "dgemm_tflops_measured": dgemm,
+                      "frac_of_measured_dgemm": tf / dgemm, "frac_of_nominal_1.25": tf / 1.25,
+                      "ecc_reference": ref, "energy_error": (e - ref) if ref is not None else None,
+                      "cpu_reference": cpu,
+                      "speedup_vs_cpu_reference": (cpu["s_per_iter"] / s_iter) if cpu else None}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -462,7 +513,10 @@ def main():
                     help="run every iteration in this precision stage (profiling of that stage)")
     ap.add_argument("--converge-iters", type=int, default=60,
                     help="untimed iterations allowed after the timed ones to reach the floor")
-    ap.add_argument("--mode", default="ccsd", choices=["ccsd", "triples", "adjoint", "term"],
+    ap.add_argument("--fp64-maxiter", type=int, default=60,
+                    help="fp64cfg2 mode: iteration limit of the FP64 solve")
+    ap.add_argument("--mode", default="ccsd",
+                    choices=["ccsd", "triples", "adjoint", "term", "fp64cfg2"],
                     help="ccsd: the benchmark line; triples / adjoint: the (T) and adjoint "
                          "measurements at no=30,nv=240 and no=20,nv=180; term: one residual "
                          "contraction (--term) alone at --no/--nv")
@@ -491,7 +545,8 @@ def main():
         import torch
         dev = torch.device("cuda:%d" % local)
         torch.cuda.set_device(dev)
-        {"triples": triples_mode, "adjoint": adjoint_mode, "term": term_mode}[args.mode](args, dev)
+        {"triples": triples_mode, "adjoint": adjoint_mode, "term": term_mode,
+         "fp64cfg2": fp64cfg2_mode}[args.mode](args, dev)
         return
 
     import numpy as np

@@ -229,6 +229,23 @@ int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, 
 int pcg_ladder_pm_assemble(const double* Gp, const double* Gm, long long no, long long nv,
                            double* h, void* stream);
 
+/* (T) densities and Lambda sources, FP64 (t3_density, pycc/cctriples.py:1063-1157), the two
+ * elementwise steps of one ordered triple (i, j, k):
+ * pcg_t3_ijk_f64: M3 = t3c_ijk / D and N3 = t3d_ijk / D (pycc/cctriples.py:27-72, :108-147)
+ *   from the connected partials P[3][nv^3] (W[a,b,c] = P1[c][a][b] + P2[b][a][c] +
+ *   P3[a][b][c], the (T) energy's layout), eps (nmo), <ij|ab> [no][no][nv][nv], t1, t2 and
+ *   the occupied-virtual Fock block fov [no][nv] (NULL when zero); D = e_i + e_j + e_k -
+ *   e_a - e_b - e_c.
+ * pcg_t3_density_terms_f64: with sym(X)_abc = 8X_abc - 4X_bac - 4X_acb - 4X_cba + 2X_cab +
+ *   2X_bca: A = sym(2 M3 + N3), S = sym(M3 + N3), Z = 2M_abc - 2M_acb - M_bac + M_bca,
+ *   Ma = M_abc - M_cba, Mb = 2M_abc - M_acb - M_cba, Mc = 2M_abc - 2M_bac.
+ * All arrays contiguous FP64 on the device. */
+int pcg_t3_ijk_f64(const double* P, const double* eps, int i, int j, int k, int no, int nv,
+                   const double* Woovv, const double* t1, const double* t2, const double* fov,
+                   double* M3, double* N3, void* stream);
+int pcg_t3_density_terms_f64(const double* M3, const double* N3, int nv, double* A, double* S,
+                             double* Z, double* Ma, double* Mb, double* Mc, void* stream);
+
 /* Grouped segmented BF16 GEMM with FP32 output, the connected-triples builder of the (T)
  * correction (t3c_ijk, pycc/cctriples.py:56-67, for a batch of triples).  Group g computes
  *   C[out_g + m*ldm + n*ldn] = sum_s A[amap_gs][arow_gs + m, :] . B[bmap_gs][brow_gs + n, :]

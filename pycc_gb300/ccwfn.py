@@ -162,8 +162,8 @@ class CCwfn:
         if 'frozen_core' in kwargs:
             raise TypeError("the 'frozen_core' argument was removed; the frozen core is taken "
                             "from the SCF reference")
-        for name, what in (('make_t3_density', "(T) densities"),
-                           ('store_triples', "stored CC3 triples"),
+        self.make_t3_density = bool(kwargs.pop('make_t3_density', False))
+        for name, what in (('store_triples', "stored CC3 triples"),
                            ('field', "a finite field"),
                            ('localize_occ', "localised occupied orbitals")):
             if kwargs.pop(name, False):
@@ -182,7 +182,7 @@ class CCwfn:
         if local_mos not in ('PIPEK_MEZEY', 'BOYS'):
             raise InvalidKeywordError('local_mos', local_mos, ['PIPEK_MEZEY', 'BOYS'])
         self.local_mos = local_mos
-        self.make_t3_density = self.store_triples = self.field = False
+        self.store_triples = self.field = False
         # for CCSD the flag changes nothing (the reference's CC3 triples read it); complex
         # amplitudes are recognised by their dtype
         self.real_time = bool(kwargs.pop('real_time', False))
@@ -466,6 +466,17 @@ class CCwfn:
         _lib.call("pcg_lincomb_f64", ptrs, coef, len(xs), out.numel(), out.data_ptr(), self._st())
         return out
 
+    def t3_density(self):
+        """(T) contributions to the densities and the Lambda residuals (``Doo, Dvv, Dov,
+        Goovv, Gooov, Gvvvo, S1, S2``), cached as attributes as the reference caches them
+        (``pycc/ccwfn.py:1819-1829``); returns the (T) energy.  FP64 on the GPU
+        (``pycc_gb300.triples_density``)."""
+        from .triples_density import t3_density
+        et, dens = t3_density(self)
+        for name, value in dens.items():
+            setattr(self, name, value)
+        return et
+
     def mixed_engine(self):
         if self._mixed is None:
             from .mixed import MixedResidual
@@ -634,8 +645,11 @@ class CCwfn:
                     # of the amplitude buffer records every later in-place change)
                     self._tape_version = self._amps._version
                 if self.model == 'CCSD(T)':
-                    from .triples import t_energy
-                    et = t_energy(self)
+                    if self.make_t3_density:
+                        et = self.t3_density()
+                    else:
+                        from .triples import t_energy
+                        et = t_energy(self)
                     self.et = et
                     ecc = ecc + et
                     self.ecc = ecc

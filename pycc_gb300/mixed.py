@@ -279,8 +279,8 @@ class MixedResidual:
 
     def timed(self, name, fn, *args):
         """Run one term; with ``self.profile`` set, CUDA events on the launching stream
-        around it (pack + GEMM + assembly) join the per-term table, and an NVTX range names
-        it for profilers."""
+        around it (pack + GEMM + assembly) join the per-term table, and an NVTX range named
+        ``name`` ("ladder", "hole_ladder") selects its launches for profilers."""
         torch.cuda.nvtx.range_push(name)
         if self.profile is None:
             fn(*args)
@@ -387,8 +387,8 @@ class MixedResidual:
         contract_f64('je,me->mj', t1, Fme, out=Fmj, alpha=0.5, beta=1.0)
         self.tcc('imab,mj->ijab', Operand.of('imab', t2), Operand.of('mj', Fmj), r, alpha=-1.0)
         # ladders
-        self.timed("mnab,mnij->ijab", self.hole_ladder_pairs, t1, t2, Wmnij, r)
-        self.timed("ijef,abef->ijab", self.ladder_pm, t1, t2, r, self.ladder_fmt())
+        self.timed("hole_ladder", self.hole_ladder_pairs, t1, t2, Wmnij, r)
+        self.timed("ladder", self.ladder_pm, t1, t2, r, self.ladder_fmt())
         # - t_ma (Z_mbij + <mb|ij>) - t_ie t_ma <mb|ej> - t_ie t_mb <ma|je>, the last written
         # as its (i<->j, a<->b) image - t_je t_ma <mb|ie>, which the symmetrisation
         # r2 = h + h' sums to the same residual; the o^3 v tensors are summed in Zmbij

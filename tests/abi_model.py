@@ -226,6 +226,45 @@ class ABIModel:
             else:
                 H[i, i][a, b] += np.where(strict, g, 0.5 * g)
 
+    # -- the (T) density entry points -----------------------------------------------------
+    def t3_ijk_f64(self, P, eps, i, j, k, no, nv, Woovv, t1, t2, fov, M3, N3, _st):
+        v = nv
+        Pv = flat(P, 3 * v ** 3).reshape(3, v, v, v)
+        # W[a,b,c] = P1[c][a][b] + P2[b][a][c] + P3[a][b][c]
+        W = np.einsum('cab->abc', Pv[0]) + np.einsum('bac->abc', Pv[1]) + Pv[2]
+        e = flat(eps, no + nv)
+        ev = e[no:]
+        D = e[i] + e[j] + e[k] - ev[:, None, None] - ev[None, :, None] - ev[None, None, :]
+        Wo = flat(Woovv, no * no * v * v).reshape(no, no, v, v)
+        T1 = flat(t1, no * v).reshape(no, v)
+        T2 = flat(t2, no * no * v * v).reshape(no, no, v, v)
+        n = (Wo[i, j][:, :, None] * T1[k][None, None, :] + Wo[i, k][:, None, :] * T1[j][None, :, None]
+             + Wo[j, k][None, :, :] * T1[i][:, None, None])
+        if fov:
+            Fo = flat(fov, no * v).reshape(no, v)
+            n = n + (T2[i, j][:, :, None] * Fo[k][None, None, :] + T2[i, k][:, None, :] * Fo[j][None, :, None]
+                     + T2[j, k][None, :, :] * Fo[i][:, None, None])
+        flat(M3, v ** 3)[...] = (W / D).ravel()
+        flat(N3, v ** 3)[...] = (n / D).ravel()
+
+    def t3_density_terms_f64(self, M3, N3, nv, A, S, Z, Ma, Mb, Mc, _st):
+        v = nv
+        M = flat(M3, v ** 3).reshape(v, v, v)
+        N = flat(N3, v ** 3).reshape(v, v, v)
+
+        def sym(X):   # 8 X_abc - 4 X_bac - 4 X_acb - 4 X_cba + 2 X_cab + 2 X_bca
+            return (8 * X - 4 * X.transpose(1, 0, 2) - 4 * X.transpose(0, 2, 1)
+                    - 4 * X.transpose(2, 1, 0) + 2 * np.einsum('cab->abc', X)
+                    + 2 * np.einsum('bca->abc', X))
+        sm, sn = sym(M), sym(N)
+        flat(A, v ** 3)[...] = (2 * sm + sn).ravel()
+        flat(S, v ** 3)[...] = (sm + sn).ravel()
+        flat(Z, v ** 3)[...] = (2 * M - 2 * M.transpose(0, 2, 1) - M.transpose(1, 0, 2)
+                                + np.einsum('bca->abc', M)).ravel()
+        flat(Ma, v ** 3)[...] = (M - M.transpose(2, 1, 0)).ravel()
+        flat(Mb, v ** 3)[...] = (2 * M - M.transpose(0, 2, 1) - M.transpose(2, 1, 0)).ravel()
+        flat(Mc, v ** 3)[...] = (2 * M - 2 * M.transpose(1, 0, 2)).ravel()
+
     # -- the (T) entry points ------------------------------------------------------------------
     PART_LEN = 4              # the model's per-triple partial-sum length in FP32 mode
 

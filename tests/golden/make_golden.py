@@ -12,7 +12,7 @@ Hamiltonian of ``pycc_gb300.synth``.  It then runs the reference's own
 
 Usage::
 
-    PYCC_REF=<reference tree> PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian] [--no-complex] [--no-hbar]
+    PYCC_REF=<reference tree> PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py [--o20v180] [--no-o5v19] [--no-jacobian] [--no-complex] [--no-hbar] [--no-t3density]
 
 The no=20, nv=180 fixtures need ~30 GB of host RAM and several minutes.
 """
@@ -174,6 +174,23 @@ def gen_o5v19_hbar(pycc):
     print("o5v19_hbar: " + "  ".join("|%s| = %.6e" % (n, np.linalg.norm(out[n])) for n in names))
 
 
+def gen_o5v19_t3density(pycc):
+    """The reference's (T) densities and Lambda sources (``t3_density``,
+    pycc/cctriples.py:1063-1157) at its converged no=5, nv=19 amplitudes."""
+    no, nv, seed = WORKLOADS["o5v19"]
+    fac = SyntheticFactors(no, nv, seed)
+    F, ERI, L = fac.hamiltonian()
+    w = make_ref_ccwfn(pycc, F, ERI, L, no, nv)
+    quiet(w.solve_cc, 1e-12, 1e-12, 100, 8, 1)
+    from pycc.cctriples import t3_density
+    et, dens = t3_density(w.o, w.v, no, nv, w.t1, w.t2, F, ERI, L, w.contract)
+    out = {"et": float(et), "t1": w.t1, "t2": w.t2}
+    out.update({k: np.asarray(x) for k, x in dens.items()})
+    np.savez_compressed(os.path.join(HERE, "o5v19_t3density.npz"), **out)
+    print("o5v19_t3density: E(T) = %.15f  " % et
+          + "  ".join("|%s| = %.6e" % (k, np.linalg.norm(x)) for k, x in dens.items()))
+
+
 def gen_o5v19_complex(pycc):
     """The reference's residual at complex amplitudes and a complex Fock matrix, as its
     real-time propagation calls it (``residuals(F, t1, t2, real_time=True)``): no=5, nv=19,
@@ -246,6 +263,7 @@ def main():
     ap.add_argument("--no-jacobian", action="store_true")
     ap.add_argument("--no-complex", action="store_true")
     ap.add_argument("--no-hbar", action="store_true")
+    ap.add_argument("--no-t3density", action="store_true")
     args = ap.parse_args()
     pycc = import_reference()
     if not args.no_o5v19:
@@ -256,6 +274,8 @@ def main():
         gen_o5v19_complex(pycc)
     if not args.no_hbar:
         gen_o5v19_hbar(pycc)
+    if not args.no_t3density:
+        gen_o5v19_t3density(pycc)
     if args.o20v180:
         gen_o20v180(pycc, solve=False, coupling=1.0, name="o20v180_raw.npz")
         gen_o20v180(pycc, solve=True, coupling="matched", name="o20v180.npz")

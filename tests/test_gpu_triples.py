@@ -124,3 +124,25 @@ def test_tc_triples_mid_size_vs_fp64(cuda):
     etc = t_energy_tc(w, batch=32)
     print("(T) no=10 nv=80: fp64 %.12f tc %.12f diff %.2e" % (e64, etc, etc - e64))
     assert abs(etc - e64) < 1e-6
+
+
+def test_t3_density_vs_reference(cuda, ham_o5v19):
+    """(T) densities and Lambda sources on the GPU (FP64) against the reference's own
+    t3_density (o5v19_t3density.npz): every block to 1e-12 relative, E(T) to 1e-12; and the
+    CCSD(T) solve with make_t3_density=True returns the same E(T)."""
+    from conftest import golden
+    g = golden("o5v19_t3density.npz")
+    _, F, ERI, L = ham_o5v19
+    H = pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device=cuda)
+    w = pg.CCwfn(H, model="CCSD(T)", make_t3_density=True)
+    w.t1 = torch.from_numpy(g["t1"]).to(cuda)
+    w.t2 = torch.from_numpy(np.ascontiguousarray(g["t2"])).to(cuda)
+    et = w.t3_density()
+    assert abs(et - float(g["et"])) < 1e-12
+    for name in ("Doo", "Dvv", "Dov", "Goovv", "Gooov", "Gvvvo", "S1", "S2"):
+        got = getattr(w, name).cpu().numpy()
+        assert got.shape == g[name].shape, name
+        assert np.abs(got - g[name]).max() <= 1e-12 * np.abs(g[name]).max(), name
+    w2 = pg.CCwfn(H, model="CCSD(T)", make_t3_density=True)
+    e = w2.solve_cc(1e-12, 1e-12, 100)
+    assert abs(w2.et - float(g["et"])) < 1e-10 and hasattr(w2, "Gvvvo")

@@ -84,7 +84,8 @@ def test_reference_constructor_options(model, ham_o5v19):
                  real_time=False, local=None, local_cutoff=1e-5, it2_opt=True, filter=False,
                  localize_occ=False, local_mos="boys", orbital_basis="spatial", quiet=True)
     assert w.model == "CCSD" and w.local_mos == "BOYS" and w.make_t3_density is False
-    for kw in ({"make_t3_density": True}, {"field": True},
+    assert pg.CCwfn(H, model="CCSD(T)", make_t3_density=True).make_t3_density is True
+    for kw in ({"field": True},
                {"store_triples": True}, {"localize_occ": True}, {"local": "PNO"},
                {"model": "CC3"}, {"orbital_basis": "spinorbital"}, {"device": "CPU"}):
         with pytest.raises(NotImplementedError):

@@ -84,3 +84,24 @@ def test_reference_entry_point_names(model, ham_o5v19, golden_o5v19):
     w = converged(ham_o5v19, golden_o5v19)
     assert abs(t_tjl(w) - float(golden_o5v19["et_tjl"])) < 1e-13
     assert abs(t_vikings(w) - float(golden_o5v19["et_vikings"])) < 1e-13
+
+
+def test_t3_density_vs_reference(monkeypatch, ham_o5v19):
+    """The (T) densities and Lambda sources (t3_density, pycc/cctriples.py:1063-1157) planned
+    by the engine, through the numpy model of the entry points, against the reference's own
+    (o5v19_t3density.npz): every block to 1e-12 relative, E(T) to 1e-13."""
+    import abi_model
+    from conftest import golden
+    abi_model.install(monkeypatch)
+    g = golden("o5v19_t3density.npz")
+    _, F, ERI, L = ham_o5v19
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, 5, L=L, device="cpu"), model="CCSD(T)",
+                 make_t3_density=True)
+    w.t1 = torch.from_numpy(g["t1"].copy())
+    w.t2 = torch.from_numpy(g["t2"].copy())
+    et = w.t3_density()
+    assert abs(et - float(g["et"])) < 1e-13
+    for name in ("Doo", "Dvv", "Dov", "Goovv", "Gooov", "Gvvvo", "S1", "S2"):
+        got = getattr(w, name).numpy()
+        assert got.shape == g[name].shape, name
+        assert np.abs(got - g[name]).max() <= 1e-12 * np.abs(g[name]).max(), name
