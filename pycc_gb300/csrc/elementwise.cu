@@ -168,30 +168,37 @@ __global__ void update_inv_kernel(double* __restrict__ t, const double* __restri
   if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
+// One warp per row (i, j, a) of the doubles: the lanes walk b, so t2 and L are read in
+// coalesced runs (L's b stride is 1 for the resident block) and the row's index
+// decomposition and t_ia are paid once per row; two FP64 FMAs per element, the singles part
+// by the first rows' warps.
 __global__ void energy_kernel(const double* __restrict__ fov, long long fs0, long long fs1,
                               const double* __restrict__ L, Strides4 ls,
                               const double* __restrict__ t1, const double* __restrict__ t2,
                               long long no, long long nv, double* __restrict__ part) {
-  long long n1 = no * nv, total = n1 + no * no * nv * nv;
+  const long long n1 = no * nv;
+  const int lane = threadIdx.x & 31;
+  const long long warp0 = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   double acc = 0.0;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (long long)gridDim.x * blockDim.x) {
-    // index decomposition in 32-bit arithmetic (o^2 v^2 < 2^31, checked by the host)
-    const unsigned v32 = (unsigned)nv, o32 = (unsigned)no;
-    if (idx < n1) {
-      const unsigned x = (unsigned)idx;
-      const long long a = x % v32, i = x / v32;
-      acc += 2.0 * fov[i * fs0 + a * fs1] * t1[idx];
-    } else {
-      const long long q = idx - n1;
-      unsigned r = (unsigned)q;
-      const long long b = r % v32;
-      r /= v32;
-      const long long a = r % v32;
-      r /= v32;
-      const long long j = r % o32, i = r / o32;
-      double tau = t2[q] + t1[i * nv + a] * t1[j * nv + b];
-      acc += tau * L[i * ls.o[0] + j * ls.o[1] + a * ls.o[2] + b * ls.o[3]];
+  for (long long x = warp0 * 32 + lane; x < n1; x += nwarps * 32) {
+    const long long a = x % nv, i = x / nv;
+    acc += 2.0 * fov[i * fs0 + a * fs1] * t1[x];
+  }
+  const long long rows = no * no * nv;  // (i, j, a); o^2 v^2 < 2^31 (host check)
+  for (long long r = warp0; r < rows; r += nwarps) {
+    unsigned q = (unsigned)r;
+    const long long a = q % (unsigned)nv;
+    q /= (unsigned)nv;
+    const long long j = q % (unsigned)no, i = q / (unsigned)no;
+    const double tia = t1[i * nv + a];
+    const double* t2r = t2 + r * nv;
+    const double* Lr = L + i * ls.o[0] + j * ls.o[1] + a * ls.o[2];
+    const double* t1j = t1 + j * nv;
+    const long long sb = ls.o[3];
+    for (long long b = lane; b < nv; b += 32) {
+      const double tau = fma(tia, t1j[b], t2r[b]);
+      acc = fma(tau, Lr[b * sb], acc);
     }
   }
   acc = block_sum(acc);

@@ -563,7 +563,9 @@ __device__ __forceinline__ V pack_ld(const double* q) {
   else return f64_to_f32(*q);
 }
 
-template <typename V, bool KF>
+// PROD: the operand may have the product sources P*Q / R*S (compiled out otherwise, which
+// keeps the plain gathers within the register budget of eight resident blocks per SM)
+template <typename V, bool KF, bool PROD = true>
 __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t, long long r0,
                                                long long k0) {
   const int tid = threadIdx.x;
@@ -605,11 +607,11 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
   long long f[kPackSrc] = {0, 0, 0, 0, 0, 0};
   if (p.X) f[0] = KF ? t.kof[0][fx] : t.rof[0][fx];
   if (p.Y) f[1] = KF ? t.kof[1][fx] : t.rof[1][fx];
-  if (p.P) {
+  if (PROD && p.P) {
     f[2] = KF ? t.kof[2][fx] : t.rof[2][fx];
     f[3] = KF ? t.kof[3][fx] : t.rof[3][fx];
   }
-  if (p.R2) {
+  if (PROD && p.R2) {
     f[4] = KF ? t.kof[4][fx] : t.rof[4][fx];
     f[5] = KF ? t.kof[5][fx] : t.rof[5][fx];
   }
@@ -624,8 +626,9 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
       auto wof = [&](int src) { return KF ? t.rof[src][wv] : t.kof[src][wv]; };
       if (p.X) v = a * pack_ld<V>(p.X + f[0] + wof(0));
       if (p.Y) v += b * pack_ld<V>(p.Y + f[1] + wof(1));
-      if (p.P) v += c * pack_ld<V>(p.P + f[2] + wof(2)) * pack_ld<V>(p.Q + f[3] + wof(3));
-      if (p.R2) v += d * pack_ld<V>(p.R2 + f[4] + wof(4)) * pack_ld<V>(p.S2 + f[5] + wof(5));
+      if (PROD && p.P) v += c * pack_ld<V>(p.P + f[2] + wof(2)) * pack_ld<V>(p.Q + f[3] + wof(3));
+      if (PROD && p.R2)
+        v += d * pack_ld<V>(p.R2 + f[4] + wof(4)) * pack_ld<V>(p.S2 + f[5] + wof(5));
       if (p.k_w) v *= KF ? t.kw[fx] : t.kw[wv];
     }
     vals[u] = v;
@@ -643,13 +646,14 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
 
 // BF16 / split-BF16x3 from an FP32 tile: two adjacent K entries per thread, written as one
 // bf16x2 word (K offsets are even: Kp and k0 are multiples of 64).
-// eight resident blocks per SM (32 registers): the pack waits on memory latency, and the
-// extra blocks hide more of it than the few spilled registers cost
-template <bool KF>
-__global__ void __launch_bounds__(PACK_THREADS, 8) pack_bf16_kernel(const PackArgs p) {
+// Without product sources: eight resident blocks per SM (32 registers), since the pack waits
+// on memory latency and the extra blocks hide more of it.  With them: five (48 registers),
+// where the six sources' offsets would otherwise spill.
+template <bool KF, bool PROD>
+__global__ void __launch_bounds__(PACK_THREADS, PROD ? 5 : 8) pack_bf16_kernel(const PackArgs p) {
   __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
-  pack_tile_load<float, KF>(p, t, r0, k0);
+  pack_tile_load<float, KF, PROD>(p, t, r0, k0);
   __nv_bfloat162* hi = reinterpret_cast<__nv_bfloat162*>(p.hi);
   __nv_bfloat162* lo = reinterpret_cast<__nv_bfloat162*>(p.lo);
   static_assert(TK == 64, "a warp writes one 64-entry row of the tile");
@@ -970,10 +974,15 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
     else
       pack_bf16x6_kernel<false><<<grid, PACK_THREADS, 0, st>>>(p);
   } else {
-    if (kfast)
-      pack_bf16_kernel<true><<<grid, PACK_THREADS, 0, st>>>(p);
+    const bool prod = P || R;
+    if (kfast && prod)
+      pack_bf16_kernel<true, true><<<grid, PACK_THREADS, 0, st>>>(p);
+    else if (kfast)
+      pack_bf16_kernel<true, false><<<grid, PACK_THREADS, 0, st>>>(p);
+    else if (prod)
+      pack_bf16_kernel<false, true><<<grid, PACK_THREADS, 0, st>>>(p);
     else
-      pack_bf16_kernel<false><<<grid, PACK_THREADS, 0, st>>>(p);
+      pack_bf16_kernel<false, false><<<grid, PACK_THREADS, 0, st>>>(p);
   }
   PCG_CHECK_LAUNCH("pcg_pack_operand");
   return 0;
