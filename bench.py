@@ -703,16 +703,24 @@ def main():
     t1h = w.t1.detach().cpu().pin_memory()
     t2h = w.t2.detach().cpu().pin_memory()
     e2e_modes = []
+    e2e_phases = []
 
     def e2e_step(k):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        ev[0].record()
         w.t1.copy_(t1h, non_blocking=True)
         w.t2.copy_(t2h, non_blocking=True)
+        ev[1].record()
         w.iterate(diis, k)
+        ev[2].record()
         w.diis_step(diis, k)
+        ev[3].record()
         t1h.copy_(w.t1, non_blocking=True)
         t2h.copy_(w.t2, non_blocking=True)
+        ev[4].record()
         torch.cuda.current_stream().synchronize()
         e2e_modes.append(w.mixed_engine().mode_name())
+        e2e_phases.append([ev[q].elapsed_time(ev[q + 1]) for q in range(4)])
 
     if args.e2e_steps > 0:
         n += 1
@@ -790,6 +798,9 @@ def main():
                 "what": "one CCwfn iteration (residual, update, energy, DIIS) per step, t1/t2 "
                         "copied in from pinned host memory and back out every step",
                 "modes": e2e_modes[-args.e2e_steps:],
+                "phases_ms": dict(zip(("h2d", "iterate", "diis", "d2h"),
+                                      np.mean(e2e_phases[-args.e2e_steps:], axis=0).round(2)
+                                      .tolist())) if args.e2e_steps > 0 else None,
                 "ms_per_step": e2e_ms} if args.e2e_steps > 0 else None,
         "gpu_launches": launches, "clocks": clocks, "setup_s": setup_s,
         "gemm_ms_per_iter": gemm_ms,

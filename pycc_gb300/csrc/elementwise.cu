@@ -196,10 +196,20 @@ __global__ void energy_kernel(const double* __restrict__ fov, long long fs0, lon
     const double* Lr = L + i * ls.o[0] + j * ls.o[1] + a * ls.o[2];
     const double* t1j = t1 + j * nv;
     const long long sb = ls.o[3];
-    for (long long b = lane; b < nv; b += 32) {
-      const double tau = fma(tia, t1j[b], t2r[b]);
-      acc = fma(tau, Lr[b * sb], acc);
+    // four elements per lane in flight: the loads of a step are issued before its FMAs
+    long long b = lane;
+    double acc1 = 0.0, acc2 = 0.0, acc3 = 0.0;
+    for (; b + 96 < nv; b += 128) {
+      const double x0 = t2r[b], x1 = t2r[b + 32], x2 = t2r[b + 64], x3 = t2r[b + 96];
+      const double l0 = Lr[b * sb], l1 = Lr[(b + 32) * sb], l2 = Lr[(b + 64) * sb],
+                   l3 = Lr[(b + 96) * sb];
+      acc = fma(fma(tia, t1j[b], x0), l0, acc);
+      acc1 = fma(fma(tia, t1j[b + 32], x1), l1, acc1);
+      acc2 = fma(fma(tia, t1j[b + 64], x2), l2, acc2);
+      acc3 = fma(fma(tia, t1j[b + 96], x3), l3, acc3);
     }
+    for (; b < nv; b += 32) acc = fma(fma(tia, t1j[b], t2r[b]), Lr[b * sb], acc);
+    acc += (acc1 + acc2) + acc3;
   }
   acc = block_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = acc;

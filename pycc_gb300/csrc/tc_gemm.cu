@@ -55,6 +55,7 @@ struct Args {
   long long M, N;
   long long mt, nt;  // output tiles along M and N
   int gm;            // M tiles per raster group (see decode_tile)
+  int bs;            // columns per N tile: BN or less, a multiple of 16 (see pcg_tc_gemm)
   int splits;        // K splits across CTAs (FP64 atomics in the epilogue when > 1)
   int kb_per_split;  // K blocks of one split
   int nkb_total;     // K blocks of the whole K range
@@ -71,6 +72,7 @@ struct Args {
   const long long* col_map;   // optional per-column C offsets (replaces en)
   const double* col_scale;    // optional per-column multipliers
   int atomic_out;
+  int red_out;  // one FP64 flush per tile (short K): add into C by reductions when beta is 1
   int* status;
 };
 
@@ -161,24 +163,13 @@ __device__ __forceinline__ int epi_col(int h, int jj) {
 // Column offsets are 32-bit (the host checks that every column offset of C is below 2^31;
 // the row offset stays 64-bit), so a batch's offsets stay in registers next to its
 // accumulator values and old C values.
-template <int W, bool SPLIT = false>
+template <int W>
 __device__ __forceinline__ void epi_batch(uint32_t taddr, const int* co, const float* sc,
                                           bool row_ok, double* crow, float ascale,
-                                          double cscale, bool need_old, int atomic_out,
-                                          uint32_t small_addr = 0, bool add_small = false) {
+                                          double cscale, bool need_old, int atomic_out) {
   uint32_t r[W];
   if constexpr (W == 32) tmem_ld32(taddr, r);
   else tmem_ld16(taddr, r);
-  if constexpr (SPLIT) {
-    if (add_small) {  // leading chunk sum + the tile's small-product sum, one FP32 rounding
-      uint32_t r2[W];
-      if constexpr (W == 32) tmem_ld32(small_addr, r2);
-      else tmem_ld16(small_addr, r2);
-#pragma unroll
-      for (int j = 0; j < W; ++j)
-        r[j] = __float_as_uint(__uint_as_float(r[j]) + __uint_as_float(r2[j]));
-    }
-  }
   if (!row_ok) return;
   int cj[W];
   double old[W];
@@ -199,6 +190,25 @@ __device__ __forceinline__ void epi_batch(uint32_t taddr, const int* co, const f
     else
       crow[c] = fma(cscale, old[j], v);
   }
+}
+
+// Split accumulators, last chunk of a tile: the leading chunk sum + the tile's small-product
+// sum (one FP32 rounding) written back over the leading buffer, so that the small
+// accumulator is free for the next tile's MMAs before this chunk's FP64 epilogue runs.
+template <int W>
+__device__ __forceinline__ void tmem_fold(uint32_t lead, uint32_t small) {
+  uint32_t r[W], s[W];
+  if constexpr (W == 32) {
+    tmem_ld32(lead, r);
+    tmem_ld32(small, s);
+  } else {
+    tmem_ld16(lead, r);
+    tmem_ld16(small, s);
+  }
+#pragma unroll
+  for (int j = 0; j < W; ++j) r[j] = __float_as_uint(__uint_as_float(r[j]) + __uint_as_float(s[j]));
+  if constexpr (W == 32) tmem_st32(lead, r);
+  else tmem_st16(lead, r);
 }
 
 // Persistent, warp-specialised tcgen05 GEMM.  Each CTA walks the tiles t = blockIdx.x,
@@ -269,7 +279,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         int split;
         long long m0, nti;
         decode_tile(p, t, split, m0, nti);
-        const int n0 = (int)(nti * BN);
+        const int n0 = (int)(nti * p.bs);
         const int kb0 = split * p.kb_per_split;
         const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
         for (int c0 = kb0; c0 < kb1 && !stop; c0 += p.kb_chunk) {
@@ -331,10 +341,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
           }
           tc_fence_after();
         }
-        // the last N tile of a ragged N multiplies only its present columns (rounded up to
-        // the MMA's multiple of 16); the columns beyond are never stored
-        const long long nleft = p.N - nti * BN;
-        const uint32_t nmma = nleft >= BN ? (uint32_t)BN : (uint32_t)((nleft + 15) & ~15LL);
+        // a tile multiplies its bs columns; the last N tile of a ragged N only its present
+        // columns (rounded up to the MMA's multiple of 16).  Accumulator columns beyond are
+        // never stored.
+        const long long nleft = p.N - nti * p.bs;
+        const uint32_t nmma =
+            nleft >= p.bs ? (uint32_t)p.bs : (uint32_t)((nleft + 15) & ~15LL);
         const uint32_t idesc_t = (idesc & ~(0x3Fu << 17)) | ((nmma >> 3) << 17);
         for (int c0 = kb0; c0 < kb1 && !stop; c0 += p.kb_chunk, ++u) {
           const int c1 = min(c0 + p.kb_chunk, kb1);
@@ -417,7 +429,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       int split;
       long long m0, nti;
       decode_tile(p, t, split, m0, nti);
-      const long long n0 = nti * BN;
+      const long long n0 = nti * p.bs;
       const int kb0 = split * p.kb_per_split;
       const int kb1 = min(p.nkb_total, kb0 + p.kb_per_split);
       const long long row = m0 + q * 32 + lane;
@@ -426,8 +438,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
       const float ascale = (p.fp8 && row_ok) ? p.a_scale[row] : 1.0f;
       __syncwarp();  // the previous tile's column offsets are no longer read
       for (int j = lane; j < HB; j += 32) {
-        const long long c = n0 + epi_col<BN>(h, j);
-        const bool in = c < p.N;
+        const int cj = epi_col<BN>(h, j);
+        const long long c = n0 + cj;
+        const bool in = cj < p.bs && c < p.N;
         colofs[j] = in ? (int)(p.col_map ? p.col_map[c] : epi_offset(p.en, c)) : -1;
         double sc = p.alpha;
         if (in && p.fp8) sc *= (double)p.b_scale[c];
@@ -455,29 +468,38 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
         }
         tc_fence_after();
         const double cscale = first ? p.beta : 1.0;  // beta applies once per tile
-        const bool need_old = !p.atomic_out && cscale != 0.0;
-        const bool last = c0 + p.kb_chunk >= kb1;   // SPLIT: add the small products now
+        // adds into C as fire-and-forget reductions (split K, or one flush per tile with C's
+        // scale 1: the warp then waits on no load of the old C values)
+        const int red = p.atomic_out || (p.red_out && cscale == 1.0);
+        const bool need_old = !red && cscale != 0.0;
         double* crow = p.C + roff;
         const uint32_t lanes = (uint32_t)(q * 32) << 16;
         const uint32_t tbase = tmem + lanes + (uint32_t)(b * L::ACC);
-        const uint32_t sbase = tmem + lanes + (uint32_t)L::SMALL;
         constexpr int NFULL = BN / 64;  // whole 32-column blocks per warp
+        if constexpr (SPLIT) {
+          if (c0 + p.kb_chunk >= kb1) {  // the tile's last chunk: fold in the small products
+            const uint32_t sbase = tmem + lanes + (uint32_t)L::SMALL;
+#pragma unroll 1
+            for (int fb = 0; fb < NFULL; ++fb)
+              tmem_fold<32>(tbase + 32 * (2 * fb + h), sbase + 32 * (2 * fb + h));
+            if constexpr (BN % 64 != 0)
+              tmem_fold<16>(tbase + (BN - 32) + 16 * h, sbase + (BN - 32) + 16 * h);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sempty[0]);
+          }
+        }
 #pragma unroll 1
         for (int fb = 0; fb < NFULL; ++fb)
-          epi_batch<32, SPLIT>(tbase + 32 * (2 * fb + h), colofs + 32 * fb, colsc + 32 * fb,
-                               row_ok, crow, ascale, cscale, need_old, p.atomic_out,
-                               sbase + 32 * (2 * fb + h), last);
+          epi_batch<32>(tbase + 32 * (2 * fb + h), colofs + 32 * fb, colsc + 32 * fb, row_ok,
+                        crow, ascale, cscale, need_old, red);
         if constexpr (BN % 64 != 0)  // BN = 96, 160, 224: the last block split 16 / 16
-          epi_batch<16, SPLIT>(tbase + (BN - 32) + 16 * h, colofs + 32 * NFULL,
-                               colsc + 32 * NFULL, row_ok, crow, ascale, cscale, need_old,
-                               p.atomic_out, sbase + (BN - 32) + 16 * h, last);
+          epi_batch<16>(tbase + (BN - 32) + 16 * h, colofs + 32 * NFULL, colsc + 32 * NFULL,
+                        row_ok, crow, ascale, cscale, need_old, red);
         first = false;
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) {
-          mbar_arrive(&tempty[b]);
-          if (SPLIT && last) mbar_arrive(&sempty[0]);
-        }
+        if (lane == 0) mbar_arrive(&tempty[b]);
       }
     }
   }
@@ -607,14 +629,7 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
   long long f[kPackSrc] = {0, 0, 0, 0, 0, 0};
   if (p.X) f[0] = KF ? t.kof[0][fx] : t.rof[0][fx];
   if (p.Y) f[1] = KF ? t.kof[1][fx] : t.rof[1][fx];
-  if (PROD && p.P) {
-    f[2] = KF ? t.kof[2][fx] : t.rof[2][fx];
-    f[3] = KF ? t.kof[3][fx] : t.rof[3][fx];
-  }
-  if (PROD && p.R2) {
-    f[4] = KF ? t.kof[4][fx] : t.rof[4][fx];
-    f[5] = KF ? t.kof[5][fx] : t.rof[5][fx];
-  }
+  // phase 1: the sources read from DRAM (X, Y), all gathers of the thread in flight
   V vals[PER];
 #pragma unroll
   for (int u = 0; u < PER; ++u) {
@@ -626,9 +641,6 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
       auto wof = [&](int src) { return KF ? t.rof[src][wv] : t.kof[src][wv]; };
       if (p.X) v = a * pack_ld<V>(p.X + f[0] + wof(0));
       if (p.Y) v += b * pack_ld<V>(p.Y + f[1] + wof(1));
-      if (PROD && p.P) v += c * pack_ld<V>(p.P + f[2] + wof(2)) * pack_ld<V>(p.Q + f[3] + wof(3));
-      if (PROD && p.R2)
-        v += d * pack_ld<V>(p.R2 + f[4] + wof(4)) * pack_ld<V>(p.S2 + f[5] + wof(5));
       if (p.k_w) v *= KF ? t.kw[fx] : t.kw[wv];
     }
     vals[u] = v;
@@ -641,16 +653,48 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
     else
       t.v[fx][wv] = vals[u];
   }
+  // phase 2: the product sources P*Q and R*S (t1-sized factors, cache-resident), added to
+  // the thread's own tile entries; separate from phase 1 so that its gathers from DRAM are
+  // not held back by the registers of these.  The K multipliers are powers of two, so
+  // applying them to each part gives the same value as to the sum.
+  if constexpr (PROD) {
+    if (p.P || p.R2) {
+      if (p.P) {
+        f[2] = KF ? t.kof[2][fx] : t.rof[2][fx];
+        f[3] = KF ? t.kof[3][fx] : t.rof[3][fx];
+      }
+      if (p.R2) {
+        f[4] = KF ? t.kof[4][fx] : t.rof[4][fx];
+        f[5] = KF ? t.kof[5][fx] : t.rof[5][fx];
+      }
+#pragma unroll 4
+      for (int u = 0; u < PER; ++u) {
+        const int wv = w0 + u * STEP;
+        if (fx_ok && wv < wlim) {
+          auto wof = [&](int src) { return KF ? t.rof[src][wv] : t.kof[src][wv]; };
+          V v = 0;
+          if (p.P) v = c * pack_ld<V>(p.P + f[2] + wof(2)) * pack_ld<V>(p.Q + f[3] + wof(3));
+          if (p.R2) v += d * pack_ld<V>(p.R2 + f[4] + wof(4)) * pack_ld<V>(p.S2 + f[5] + wof(5));
+          if (p.k_w) v *= KF ? t.kw[fx] : t.kw[wv];
+          if (KF)
+            t.v[wv][fx] += v;
+          else
+            t.v[fx][wv] += v;
+        }
+      }
+    }
+  }
   __syncthreads();
 }
 
 // BF16 / split-BF16x3 from an FP32 tile: two adjacent K entries per thread, written as one
 // bf16x2 word (K offsets are even: Kp and k0 are multiples of 64).
-// Without product sources: eight resident blocks per SM (32 registers), since the pack waits
-// on memory latency and the extra blocks hide more of it.  With them: five (48 registers),
-// where the six sources' offsets would otherwise spill.
+// Eight resident blocks per SM (32 registers), since the pack waits on memory latency and
+// the extra blocks hide more of it.  The product sources are added in a second phase of the
+// tile load (PROD), which keeps that variant within the same register budget; the plain
+// variant compiles the phase out.
 template <bool KF, bool PROD>
-__global__ void __launch_bounds__(PACK_THREADS, PROD ? 5 : 8) pack_bf16_kernel(const PackArgs p) {
+__global__ void __launch_bounds__(PACK_THREADS, 8) pack_bf16_kernel(const PackArgs p) {
   __shared__ PackTile<float> t;
   const long long r0 = (long long)blockIdx.x * TR, k0 = (long long)blockIdx.y * TK;
   pack_tile_load<float, KF, PROD>(p, t, r0, k0);
@@ -810,7 +854,7 @@ int launch(const Maps& maps, Args a, cudaStream_t st) {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     attr = true;
   }
-  a.nt = (a.N + BN - 1) / BN;
+  a.nt = (a.N + a.bs - 1) / a.bs;
   const long long ntiles = a.mt * a.nt * a.splits;
   const long long grid = std::min<long long>(ntiles, num_sms());
   tc_gemm_kernel<BN, NP, SPLIT><<<(unsigned)grid, GEMM_THREADS, smem, st>>>(maps, a);
@@ -1093,6 +1137,16 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   splits = (nkb + kps - 1) / kps;
   a.mt = mt;
   a.nt = nt;
+  // N is cut into nt tiles of near-equal width (bs columns, a multiple of 16, the last tile
+  // the rest): tiles that take about the same time keep the CTAs that share an A row block
+  // in step, so they find it in L2.  A narrow last tile (820 = 5 x 160 + 20 columns) ends
+  // early and its CTA runs ahead onto other row blocks (measured on GB300 at 820 columns:
+  // the A operand read 2.5 times from DRAM, against 1.05 times at 780 = 4 x 160 + 140).
+  // bs <= BN and bs * nt >= N, so the tile count is unchanged.
+  {
+    const long long units = (N + 15) / 16;
+    a.bs = (int)(16 * ((units + nt - 1) / nt));
+  }
   // raster group: a wave of W CTAs touches gm A row blocks (BM rows) and W / gm B row
   // blocks (BN rows); gm = sqrt(W BN / BM) minimises their sum.  A narrow N (nt <= W / gm)
   // keeps the N-fastest order (gm = 1): the CTAs sharing an A row block are then adjacent
@@ -1114,6 +1168,10 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   a.kb_chunk = (fmt == kBF16x3 || fmt == kBF16x3F || fmt == kBF16x3S) ? 64
                                                                       : (fmt == kBF16x6 ? 32 : 192);
   a.atomic_out = splits > 1;
+  // a tile whose K fits one flush adds its result into C once: as a reduction the add is
+  // done at L2 and the epilogue does not wait a DRAM round trip per tile for the old values
+  // (the short-K terms are bound by that wait)
+  a.red_out = (splits == 1 && nkb <= a.kb_chunk) ? 1 : 0;
   cudaStream_t st = (cudaStream_t)stream;
   if (a.atomic_out && beta != 1.0) {
     int blocks = (int)std::min<long long>((M * N + 255) / 256, 4096);

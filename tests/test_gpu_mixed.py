@@ -25,10 +25,12 @@ def frob(a, b):
 @pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_FP8])
 @pytest.mark.parametrize("M,N,K", [(128, 64, 64), (200, 70, 100), (37, 300, 513), (64, 180, 96),
                                    (100, 210, 64), (150, 150, 64), (300, 820, 200),
-                                   (3000, 2000, 64)])
+                                   (3000, 2000, 64), (700, 1000, 128)])
 def test_gemm_exact_integers(cuda, fmt, M, N, K):
     """N = 70, 150, 180, 210, 820 select the 96-, 160-, 192- and 224-column tiles (fused
-    formats stop at 160); 3000 x 2000 walks several raster groups, the last one partial."""
+    formats stop at 160); 3000 x 2000 walks several raster groups, the last one partial.
+    N is cut into tiles of near-equal width below the tile's capacity (820 = 5 x 144 + 100
+    and 1000 = 6 x 144 + 136 in 160-column tiles, 210 = 112 + 98)."""
     g = torch.Generator(device=cuda).manual_seed(M + N + K)
     A = torch.randint(-3, 4, (M, K), generator=g, device=cuda).double()
     B = torch.randint(-3, 4, (N, K), generator=g, device=cuda).double()
@@ -113,9 +115,11 @@ def test_pack_rounding_bit_exact(cuda, fmt):
         assert torch.equal(P.lo[:, :K][fin].view(torch.int16), lo[fin].view(torch.int16))
 
 
-def test_pack_combination(cuda):
-    """a*X + b*Y + c*P*Q with permuted sources, K padding and a row table, against FP64
-    within the FP32 rounding of the operands."""
+@pytest.mark.parametrize("rows,ks", [("ij", "k"), ("k", "ij")])
+def test_pack_combination(cuda, rows, ks):
+    """a*X + b*Y + c*P*Q with permuted sources and K padding, against FP64 within the FP32
+    rounding of the operands; K along X's unit-stride index (the K-gathering pack) and rows
+    along it (the row-gathering pack)."""
     from pycc_gb300.tc import pack
     g = torch.Generator(device=cuda).manual_seed(12)
     X = torch.randn(7, 9, 70, generator=g, device=cuda, dtype=torch.float64)
@@ -123,15 +127,18 @@ def test_pack_combination(cuda):
     Pm = torch.randn(7, 70, generator=g, device=cuda, dtype=torch.float64)
     Q = torch.randn(9, generator=g, device=cuda, dtype=torch.float64)
     op = Operand("ijk", (X, "ijk"), a=2.0, Y=(Y, "jik"), b=-0.5, P=(Pm, "ik"), Q=(Q, "j"), c=0.25)
-    P = pack(op, "ij", "k", FMT_BF16X3)
+    P = pack(op, rows, ks, FMT_BF16X3)
     torch.cuda.synchronize()
     parts = (2.0 * X, -0.5 * Y.transpose(0, 1), 0.25 * Pm[:, None, :] * Q[None, :, None])
     ref = sum(parts).reshape(63, 70)
     scale = sum(q.abs() for q in parts).reshape(63, 70)
-    got = P.hi[:, :70].double() + P.lo[:, :70].double()
+    if rows == "k":
+        ref, scale = ref.T, scale.T
+    K = ref.shape[1]
+    got = P.hi[:, :K].double() + P.lo[:, :K].double()
     # split error 2^-17 of the value, FP32 combination 2^-24 of each operand (a few roundings)
     assert torch.all((got - ref).abs() <= 2.0 ** -16 * ref.abs() + 2.0 ** -21 * scale)
-    assert torch.all(P.hi[:, 70:].float() == 0) and torch.all(P.lo[:, 70:].float() == 0)
+    assert torch.all(P.hi[:, K:].float() == 0) and torch.all(P.lo[:, K:].float() == 0)
 
 
 def test_split_k_small_output(cuda):
