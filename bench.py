@@ -705,22 +705,31 @@ def main():
     e2e_modes = []
     e2e_phases = []
 
+    e2e_host = []
+
     def e2e_step(k):
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        hs = [time.perf_counter()]
         ev[0].record()
         w.t1.copy_(t1h, non_blocking=True)
         w.t2.copy_(t2h, non_blocking=True)
         ev[1].record()
+        hs.append(time.perf_counter())
         w.iterate(diis, k)
         ev[2].record()
+        hs.append(time.perf_counter())
         w.diis_step(diis, k)
         ev[3].record()
+        hs.append(time.perf_counter())
         t1h.copy_(w.t1, non_blocking=True)
         t2h.copy_(w.t2, non_blocking=True)
         ev[4].record()
+        hs.append(time.perf_counter())
         torch.cuda.current_stream().synchronize()
+        hs.append(time.perf_counter())
         e2e_modes.append(w.mixed_engine().mode_name())
         e2e_phases.append([ev[q].elapsed_time(ev[q + 1]) for q in range(4)])
+        e2e_host.append([(hs[q + 1] - hs[q]) * 1e3 for q in range(5)])
 
     if args.e2e_steps > 0:
         n += 1
@@ -801,6 +810,9 @@ def main():
                 "phases_ms": dict(zip(("h2d", "iterate", "diis", "d2h"),
                                       np.mean(e2e_phases[-args.e2e_steps:], axis=0).round(2)
                                       .tolist())) if args.e2e_steps > 0 else None,
+                "host_phases_ms": dict(zip(("h2d", "iterate", "diis", "d2h", "sync"),
+                                           np.mean(e2e_host[-args.e2e_steps:], axis=0).round(2)
+                                           .tolist())) if args.e2e_steps > 0 else None,
                 "ms_per_step": e2e_ms} if args.e2e_steps > 0 else None,
         "gpu_launches": launches, "clocks": clocks, "setup_s": setup_s,
         "gemm_ms_per_iter": gemm_ms,

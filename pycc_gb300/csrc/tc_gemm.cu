@@ -557,6 +557,10 @@ struct PackArgs {
   const long long* k_tab;    // optional [6][K] per-source K offsets (replaces k)
   const float* k_w;          // optional [K] multipliers of the K entries
   int fmt;
+  // rows walked in an order other than the output's (see pcg_pack_operand): output row of
+  // the walked row index = sum over its sub-indices x_q * out_str[q]
+  int out_perm;
+  long long out_str[kMaxSub];
 };
 
 // Tiled pack: a block handles TR rows x TK columns of K.  Row and column offsets of the
@@ -573,6 +577,7 @@ static_assert((TR * TK) % PACK_THREADS == 0, "pack tile: whole elements per thre
 
 template <typename V>
 struct PackTile {
+  long long orow[TR];  // output row of each tile row (the tile row itself unless permuted)
   long long rof[kPackSrc][TR];
   long long kof[kPackSrc][TK];
   V kw[TK];
@@ -593,12 +598,24 @@ __device__ __forceinline__ void pack_tile_load(const PackArgs& p, PackTile<V>& t
   const int tid = threadIdx.x;
   if (tid < TR) {
     long long o[kPackSrc] = {0, 0, 0, 0, 0, 0};
+    long long orow = r0 + tid;
     if (r0 + tid < p.R) {
-      if (p.row_tab)
+      if (p.row_tab) {
         for (int s = 0; s < kPackSrc; ++s) o[s] = p.row_tab[s * p.R + r0 + tid];
-      else
+      } else {
         pack_offsets(p.r, r0 + tid, o);
+        if (p.out_perm) {
+          orow = 0;
+          unsigned rr = (unsigned)(r0 + tid);
+          for (int q = p.r.n - 1; q >= 0; --q) {
+            const unsigned e = (unsigned)p.r.ext[q];
+            orow += (long long)(rr % e) * p.out_str[q];
+            rr /= e;
+          }
+        }
+      }
     }
+    t.orow[tid] = orow;
     for (int s = 0; s < kPackSrc; ++s) t.rof[s][tid] = o[s];
   } else if (tid >= TR && tid < TR + TK) {
     const int j = tid - TR;
@@ -705,7 +722,7 @@ __global__ void __launch_bounds__(PACK_THREADS, 8) pack_bf16_kernel(const PackAr
 #pragma unroll 4
   for (int rr = threadIdx.x >> 5; rr < TR; rr += PACK_THREADS / 32) {
     if (r0 + rr >= p.R) break;
-    const long long at = ((r0 + rr) * p.Kp + k0 + kk) >> 1;
+    const long long at = (t.orow[rr] * p.Kp + k0 + kk) >> 1;
     const float v0 = t.v[rr][kk], v1 = t.v[rr][kk + 1];
     const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
     hi[at] = h;
@@ -725,7 +742,7 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_bf16x6_kernel(const PackArg
   for (int e = threadIdx.x; e < TR * TK; e += PACK_THREADS) {
     const int rr = e / TK, kk = e % TK;
     if (r0 + rr >= p.R) continue;
-    const long long at = (r0 + rr) * p.Kp + k0 + kk;
+    const long long at = t.orow[rr] * p.Kp + k0 + kk;
     const double v = t.v[rr][kk];
     const __nv_bfloat16 h = __double2bfloat16(v);
     hi[at] = h;
@@ -750,7 +767,7 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_fp8_max_kernel(const PackAr
     float m = fmaxf(fabsf(t.v[rr][lane]), fabsf(t.v[rr][lane + 32]));
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if (lane == 0 && r0 + rr < p.R && m > 0.0f)
-      atomicMax(rowmax + r0 + rr, __float_as_uint(m));
+      atomicMax(rowmax + t.orow[rr], __float_as_uint(m));
   }
 }
 
@@ -778,8 +795,8 @@ __global__ void __launch_bounds__(PACK_THREADS) pack_fp8_kernel(const PackArgs p
   for (int e = threadIdx.x; e < TR * TK; e += PACK_THREADS) {
     const int rr = e / TK, kk = e % TK;
     if (r0 + rr >= p.R) continue;
-    const float inv = 1.0f / scale[r0 + rr];
-    dst[(r0 + rr) * p.Kp + k0 + kk] = __nv_fp8_e4m3(t.v[rr][kk] * inv);
+    const float inv = 1.0f / scale[t.orow[rr]];
+    dst[t.orow[rr] * p.Kp + k0 + kk] = __nv_fp8_e4m3(t.v[rr][kk] * inv);
   }
 }
 
@@ -991,6 +1008,39 @@ extern "C" int pcg_pack_operand(int fmt, int r_n, const long long* r_ext, const 
     if (p.r.s[src0][q] != 0)
       rs = (rs == 0) ? llabs(p.r.s[src0][q]) : std::min(rs, llabs(p.r.s[src0][q]));
   const int kfast = (rs == 0 || (ks != 0 && ks <= rs)) ? 1 : 0;
+  // Rows gathered along their most contiguous sub-index: when that is not the innermost
+  // one (rows (b, j) of t2[n][j][f][b]: consecutive rows are a whole (f, b) plane apart),
+  // the kernel walks the rows with it moved innermost, so that a warp's consecutive rows
+  // are consecutive addresses, and writes each walked row to its own output row.
+  p.out_perm = 0;
+  if (!kfast && !row_tab && p.r.n >= 2) {
+    int qs = -1;
+    for (int q = 0; q < p.r.n; ++q)
+      if (p.r.s[src0][q] != 0 && (qs < 0 || llabs(p.r.s[src0][q]) < llabs(p.r.s[src0][qs])))
+        qs = q;
+    if (qs >= 0 && qs != p.r.n - 1) {
+      long long ostr[kMaxSub];
+      long long run = 1;
+      for (int q = p.r.n - 1; q >= 0; --q) {  // output row strides in the given order
+        ostr[q] = run;
+        run *= p.r.ext[q];
+      }
+      PackIdx g = p.r;
+      int w = 0;
+      for (int q = 0; q < p.r.n; ++q) {
+        if (q == qs) continue;
+        g.ext[w] = p.r.ext[q];
+        for (int s = 0; s < kPackSrc; ++s) g.s[s][w] = p.r.s[s][q];
+        p.out_str[w] = ostr[q];
+        ++w;
+      }
+      g.ext[w] = p.r.ext[qs];
+      for (int s = 0; s < kPackSrc; ++s) g.s[s][w] = p.r.s[s][qs];
+      p.out_str[w] = ostr[qs];
+      p.r = g;
+      p.out_perm = 1;
+    }
+  }
   const long long gx = (p.R + TR - 1) / TR, gy = Kp / TK;
   if (gy > 65535 || p.R > 0x7fffffffLL - TR) {  // row and K indices stay below 2^31
     set_error("pcg_pack_operand: operand too large (%lld x %lld)", p.R, Kp);

@@ -276,10 +276,14 @@ class TCEngine:
         if op.key is None:
             if self.dyn_cache is None:
                 return pack(op, rows, ks, fmt, self.stream, row_tab, k_tab, k_w)
-            src = tuple((s[0].data_ptr(), tuple(s[0].stride()), s[1]) if s is not None else None
-                        for s in op.sources())
-            dkey = (src, op.a, op.b, op.c, op.d, op.labels, tuple(rows), tuple(ks), tabs,
-                    pack_format(fmt))
+            # the key is the gather itself: each source's address, and the extent and
+            # per-source strides of every row and K index, so one matrix reached through
+            # differently named labels is packed once
+            ext = op.extents()
+            src = tuple(s[0].data_ptr() if s is not None else None for s in op.sources())
+            geo = tuple((ext[c], tuple(op.strides(c))) for c in rows)
+            kgeo = tuple((ext[c], tuple(op.strides(c))) for c in ks)
+            dkey = (src, op.a, op.b, op.c, op.d, geo, kgeo, tabs, pack_format(fmt))
             hit = self.dyn_cache.get(dkey)
             if hit is None:
                 # the entry holds its source tensors and tables, so no later tensor can reuse

@@ -115,11 +115,12 @@ def test_pack_rounding_bit_exact(cuda, fmt):
         assert torch.equal(P.lo[:, :K][fin].view(torch.int16), lo[fin].view(torch.int16))
 
 
-@pytest.mark.parametrize("rows,ks", [("ij", "k"), ("k", "ij")])
+@pytest.mark.parametrize("rows,ks", [("ij", "k"), ("k", "ij"), ("ki", "j")])
 def test_pack_combination(cuda, rows, ks):
     """a*X + b*Y + c*P*Q with permuted sources and K padding, against FP64 within the FP32
-    rounding of the operands; K along X's unit-stride index (the K-gathering pack) and rows
-    along it (the row-gathering pack)."""
+    rounding of the operands; K along X's unit-stride index (the K-gathering pack), rows
+    along it (the row-gathering pack), and rows whose unit-stride sub-index is the outer one
+    (walked innermost, each walked row written to its own output row)."""
     from pycc_gb300.tc import pack
     g = torch.Generator(device=cuda).manual_seed(12)
     X = torch.randn(7, 9, 70, generator=g, device=cuda, dtype=torch.float64)
@@ -130,10 +131,10 @@ def test_pack_combination(cuda, rows, ks):
     P = pack(op, rows, ks, FMT_BF16X3)
     torch.cuda.synchronize()
     parts = (2.0 * X, -0.5 * Y.transpose(0, 1), 0.25 * Pm[:, None, :] * Q[None, :, None])
-    ref = sum(parts).reshape(63, 70)
-    scale = sum(q.abs() for q in parts).reshape(63, 70)
-    if rows == "k":
-        ref, scale = ref.T, scale.T
+    perm = ["ijk".index(c) for c in rows + ks]
+    nr = int(np.prod([X.shape["ijk".index(c)] for c in rows]))
+    ref = sum(parts).permute(*perm).reshape(nr, -1)
+    scale = sum(q.abs() for q in parts).permute(*perm).reshape(nr, -1)
     K = ref.shape[1]
     got = P.hi[:, :K].double() + P.lo[:, :K].double()
     # split error 2^-17 of the value, FP32 combination 2^-24 of each operand (a few roundings)
