@@ -229,6 +229,18 @@ int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const void* A_lo, 
 int pcg_ladder_pm_assemble(const double* Gp, const double* Gm, long long no, long long nv,
                            double* h, void* stream);
 
+/* pcg_pair_pm_assemble: the same pair form for the tau_ijef X_r,ef terms of the
+ *   intermediates (Zmbij: tau_ijef <mb|ef>, pycc/ccwfn.py:707; Wmnij: tau_ijef <mn|ef>,
+ *   pycc/ccwfn.py:596; 'ijef,mbef->mbij' / 'ijef,mnef->mnij' of ContractionBackend.__call__).
+ *   Gp: [no(no+1)/2][nrow] = 1/2 sum_{e<=f} T+_ij,ef (X_r,ef + X_r,fe) over the i <= j pairs
+ *   (row-major, with 1/2 on e = f), Gm: [no(no-1)/2][nrow] = 1/2 sum_{e<f} T-_ij,ef
+ *   (X_r,ef - X_r,fe) over the i < j pairs, so Gp + Gm = sum_ef tau_ijef X_r,ef and
+ *   Gp - Gm = sum_ef tau_jief X_r,ef.  Z[r][i][j] += Gp + Gm and Z[r][j][i] += Gp - Gm for
+ *   i < j, Z[r][i][i] += Gp.  Z: contiguous [nrow][no][no] FP64; Gm may be NULL when no = 1.
+ */
+int pcg_pair_pm_assemble(const double* Gp, const double* Gm, long long no, long long nrow,
+                         double* Z, void* stream);
+
 /* (T) densities and Lambda sources, FP64 (t3_density, pycc/cctriples.py:1063-1157), the two
  * elementwise steps of one ordered triple (i, j, k):
  * pcg_t3_ijk_f64: M3 = t3c_ijk / D and N3 = t3d_ijk / D (pycc/cctriples.py:27-72, :108-147)

@@ -57,6 +57,7 @@ SIGNATURES = {
                                    _d, _p, _d, _p, _d, _p, _p, _d, _p, _p, _p, _p, _p, _p, _p,
                                    _i64, _p, _p, _i64, _p]),
     "pcg_ladder_pm_assemble": (C.c_int, [_p, _p, _i64, _i64, _p, _p]),
+    "pcg_pair_pm_assemble": (C.c_int, [_p, _p, _i64, _i64, _p, _p]),
     "pcg_t3_ijk_f64": (C.c_int, [_p, _p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _p, _p,
                                  _p, _p, _p, _p, _p]),
     "pcg_t3_density_terms_f64": (C.c_int, [_p, _p, C.c_int, _p, _p, _p, _p, _p, _p, _p]),

@@ -64,6 +64,52 @@ __global__ void __launch_bounds__(LADDER_THREADS)
   }
 }
 
+// Block (x, i): rows r0 = 32 x .. r0 + 31 and the occupied index i; the pairs (i, j >= i)
+// in chunks of 32.  G+- are read along the row index (unit-stride) into shared memory, and
+// written along j into row i of each row's (i, j) block; the transposed element (j, i) is a
+// strided write.  Every element of Z has one writer: (x, y) with y >= x by block x, (x, y)
+// with x > y by block y.
+__global__ void __launch_bounds__(LADDER_THREADS)
+    pair_pm_assemble_kernel(const double* __restrict__ Gp, const double* __restrict__ Gm,
+                            int no, long long nrow, double* __restrict__ Z) {
+  __shared__ double sp[32][33], sm[32][33];
+  const int i = blockIdx.y;
+  const long long r0 = (long long)blockIdx.x * 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long pi = (long long)i * no - (long long)i * (i - 1) / 2;        // p(i, i)
+  const long long mi = (long long)i * (no - 1) - (long long)i * (i - 1) / 2;  // pm(i, i + 1)
+  const long long oo = (long long)no * no;
+  for (int jc = i; jc < no; jc += 32) {
+    for (int jj = warp; jj < 32; jj += LADDER_THREADS / 32) {
+      const int j = jc + jj;
+      const long long r = r0 + lane;
+      double gp = 0.0, gm = 0.0;
+      if (j < no && r < nrow) {
+        gp = Gp[(pi + (j - i)) * nrow + r];
+        if (j > i && Gm) gm = Gm[(mi + (j - i - 1)) * nrow + r];
+      }
+      sp[jj][lane] = gp;
+      sm[jj][lane] = gm;
+    }
+    __syncthreads();
+    for (int rr = warp; rr < 32; rr += LADDER_THREADS / 32) {
+      const long long r = r0 + rr;
+      const int j = jc + lane;
+      if (r < nrow && j < no) {
+        const double gp = sp[lane][rr], gm = sm[lane][rr];
+        double* zr = Z + r * oo;
+        if (j > i) {
+          zr[(long long)i * no + j] += gp + gm;
+          zr[(long long)j * no + i] += gp - gm;
+        } else {
+          zr[(long long)i * no + i] += gp;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
 }  // namespace pcg
 
@@ -88,5 +134,23 @@ extern "C" int pcg_ladder_pm_assemble(const double* Gp, const double* Gm, long l
   ladder_pm_assemble_kernel<<<grid, LADDER_THREADS, 0, (cudaStream_t)stream>>>(Gp, Gm, (int)no,
                                                                                (int)nv, h);
   PCG_CHECK_LAUNCH("pcg_ladder_pm_assemble");
+  return 0;
+}
+
+// Z[r][i][j] += Gp + Gm and Z[r][j][i] += Gp - Gm for i < j, Z[r][i][i] += Gp, with Gp
+// [no(no+1)/2][nrow] over the i <= j pairs and Gm [no(no-1)/2][nrow] over the i < j pairs
+// (row-major over i), both FP64 and contiguous; Z: the contiguous [nrow][no][no] FP64
+// array.  Gm may be NULL when it is empty (no = 1).
+extern "C" int pcg_pair_pm_assemble(const double* Gp, const double* Gm, long long no,
+                                    long long nrow, double* Z, void* stream) {
+  if (!Gp || !Z || no <= 0 || nrow <= 0 || no > 65535 || (!Gm && no > 1) ||
+      (nrow + 31) / 32 > 0x7fffffffLL) {
+    set_error("pcg_pair_pm_assemble: bad arguments (no=%lld nrow=%lld)", no, nrow);
+    return -1;
+  }
+  dim3 grid((unsigned)((nrow + 31) / 32), (unsigned)no);
+  pair_pm_assemble_kernel<<<grid, LADDER_THREADS, 0, (cudaStream_t)stream>>>(Gp, Gm, (int)no,
+                                                                             nrow, Z);
+  PCG_CHECK_LAUNCH("pcg_pair_pm_assemble");
   return 0;
 }

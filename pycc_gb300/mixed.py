@@ -59,6 +59,7 @@ class MixedResidual:
         self.profile = None       # list of (subscripts, fmt, start, end) events when set
         self._pairs = None        # output map of the i <= j pair terms
         self._pm = None           # offset tables of the ladder's pair form
+        self._kpm = {}            # K pair tables of the pair-form intermediates, per block
         self._hole_tab = None     # the pair columns of Wmnij for the hole ladder
         self._r_seed = None
         self._blocks = None       # the integral blocks the caches were built from
@@ -251,6 +252,72 @@ class MixedResidual:
                   G["-"].data_ptr() if G["-"] is not None else None, no, nv, r.data_ptr(),
                   _lib.stream_handle(self.w.stream))
 
+    def _kpair_tables(self, X):
+        """K tables of the e <= f (+) / e < f (-) pairs of the last two indices of a static
+        block X[..., e, f], for the sources X[..., e, f] and X[..., f, e], with 1/2 on e = f
+        for + (X_ee + X_ee counts it twice)."""
+        key = (tuple(X.stride()), tuple(X.shape))
+        if key in self._kpm:
+            return self._kpm[key]
+        nv = X.shape[-1]
+        se, sf = X.stride()[-2], X.stride()[-1]
+        dev = self.w.device1
+        tabs = {}
+        for sign, k in (("+", 0), ("-", 1)):
+            e, f = np.triu_indices(nv, k)
+            kt = np.zeros((6, e.size), dtype=np.int64)
+            kt[0] = e * se + f * sf
+            kt[1] = f * se + e * sf
+            kw = np.where(e == f, 0.5, 1.0).astype(np.float32) if sign == "+" else None
+            tabs[sign] = {"k": torch.from_numpy(kt).to(dev),
+                          "kw": torch.from_numpy(kw).to(dev) if kw is not None else None,
+                          "n": e.size}
+        self._kpm[key] = tabs
+        return tabs
+
+    def pair_tau(self, X, labels, name, t1, t2, out, fmt):
+        """out[r, i, j] += sum_ef tau_ijef X[r.., e, f] for a static block X whose last two
+        indices are (e, f) and whose leading ones (``labels[:-2]``) are the rows r, in the
+        ladder's symmetric / antisymmetric pair form: G+- = 1/2 sum over the e <= f (e < f)
+        pairs of T+-_ij,ef (X_ef +- X_fe), over the i <= j (i < j) pairs, then
+        ``pcg_pair_pm_assemble`` adds out_rij += G+ + G-, out_rji += G+ - G- (i < j) and
+        out_rii += G+.  T+- are the ladder's own packed operands (packed once per residual
+        call); X's pair combinations are packed once per format.  Half the tensor-core work
+        of the plain contraction (Zmbij: tau_ijef <mb|ef>, pycc/ccwfn.py:707; Wmnij:
+        tau_ijef <mn|ef>, pycc/ccwfn.py:596)."""
+        if not out.is_contiguous():
+            raise ValueError("pair_tau: the output must be contiguous")
+        no = self.w.no
+        nrow = X[..., 0, 0].numel()
+        ttabs = self._pm_tables(t1, t2, self.w.H.ERI.blocks['vvvv'])
+        ktabs = self._kpair_tables(X)
+        dev = self.w.device1
+        swapped = labels[:-2] + labels[-1] + labels[-2]
+        G = {}
+        for sign, c in (("+", 1.0), ("-", -1.0)):
+            tb, kb = ttabs[sign], ktabs[sign]
+            if tb["cols"] == 0:
+                G[sign] = None
+                continue
+            if kb["n"] == 0:
+                G[sign] = torch.zeros((tb["cols"], nrow), dtype=torch.float64, device=dev)
+                continue
+            xop = Operand(labels, (X, labels), a=1.0, Y=(X, swapped), b=c,
+                          key=("ERI", name, sign, "pairs"))
+            pa = self.tc._pack(xop, list(labels[:-2]), list(labels[-2:]), fmt, 'A',
+                               k_tab=kb["k"], k_w=kb["kw"])
+            top = Operand('ijef', (t2, 'ijef'), a=1.0, Y=(t2, 'ijfe'), b=c, P=(t1, 'ie'),
+                          Q=(t1, 'jf'), c=1.0, R=(t1, 'if'), S=(t1, 'je'), d=c)
+            pb = self.tc._pack(top, ['i', 'j'], ['e', 'f'], fmt, 'B', row_tab=tb["trow"],
+                               k_tab=tb["tk"])
+            g = torch.empty((tb["cols"], nrow), dtype=torch.float64, device=dev)
+            self.tc.run_gemm('ijef,%s->%sij%s' % (labels, labels[:-2], sign), fmt, pa, pb, g,
+                             ['p'], ['q'], 'qp', 0.5, 0.0)
+            G[sign] = g
+        _lib.call("pcg_pair_pm_assemble", G["+"].data_ptr(),
+                  G["-"].data_ptr() if G["-"] is not None else None, no, nrow, out.data_ptr(),
+                  _lib.stream_handle(self.w.stream))
+
     def hole_ladder_pairs(self, t1, t2, Wmnij, r):
         """r_ijab += 1/2 tau_mnab W_mnij (pycc/ccwfn.py:930) through the i <= j pairs only.
 
@@ -320,11 +387,11 @@ class MixedResidual:
 
     def build_Wmnij(self, t1, t2):
         o = self.w.o
-        W = self.w.H.ERI[o, o, o, o].clone()
+        W = self.w.H.ERI[o, o, o, o].clone(memory_format=torch.contiguous_format)
         self.tcc('je,mnie->mnij', Operand.of('je', t1), self.eri('ooov', 'mnie'), W)
         self.tcc('ie,mnej->mnij', Operand.of('ie', t1), self.eri('oovo', 'mnej'), W)
-        tau = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
-        self.tcc('ijef,mnef->mnij', tau, self.eri('oovv', 'mnef'), W)
+        # tau_ijef <mn|ef> in pair form
+        self.pair_tau(self.w.H.ERI.blocks['oovv'], 'mnef', 'oovv', t1, t2, W, self.fmt())
         return W
 
     def build_Wmbej(self, t1, t2):
@@ -351,8 +418,8 @@ class MixedResidual:
         contracts with t_ma, summed so that one GEMM applies them (see r_T2_half)."""
         o, v = self.w.o, self.w.v
         Z = self.w._combine(1.0, self.w.H.ERI[o, v, o, o], 0.0, None, None, record=False)
-        tau = Operand('ijef', (t2, 'ijef'), P=(t1, 'ie'), Q=(t1, 'jf'), c=1.0)
-        self.tcc('mbef,ijef->mbij', self.eri('ovvv', 'mbef'), tau, Z)
+        # tau_ijef <mb|ef> in pair form
+        self.pair_tau(self.w.H.ERI.blocks['ovvv'], 'mbef', 'ovvv', t1, t2, Z, self.fmt())
         self.tcc('ie,mbej->mbij', Operand.of('ie', t1), self.eri('ovvo', 'mbej'), Z)
         self.tcc('je,mbie->mbij', Operand.of('je', t1), self.eri('ovov', 'mbie'), Z)
         return Z

@@ -226,6 +226,22 @@ class ABIModel:
             else:
                 H[i, i][a, b] += np.where(strict, g, 0.5 * g)
 
+    def pair_pm_assemble(self, Gp, Gm, no, nrow, Z, _st):
+        """Z[r, i, j] += G+ + G-, Z[r, j, i] += G+ - G- (i < j), Z[r, i, i] += G+, as
+        pcg_pair_pm_assemble documents."""
+        gp = flat(Gp, (no * (no + 1) // 2) * nrow).reshape(-1, nrow)
+        gm = flat(Gm, (no * (no - 1) // 2) * nrow).reshape(-1, nrow) if Gm else None
+        Zv = view(Z, (nrow, no, no), (no * no, no, 1))
+        qm = 0
+        for q, (i, j) in enumerate(zip(*np.triu_indices(no))):
+            if j > i:
+                m = gm[qm] if gm is not None else 0.0
+                qm += 1
+                Zv[:, i, j] += gp[q] + m
+                Zv[:, j, i] += gp[q] - m
+            else:
+                Zv[:, i, i] += gp[q]
+
     # -- the (T) density entry points -----------------------------------------------------
     def t3_ijk_f64(self, P, eps, i, j, k, no, nv, Woovv, t1, t2, fov, M3, N3, _st):
         v = nv
