@@ -289,3 +289,49 @@ def test_ladder_pair_form_random(cuda, fmt):
     V, t1, t2, ref = _ladder_setup(cuda, 6, 45)
     got = _ladder_run(cuda, V, t1, t2, fmt)
     assert frob(got, ref) < TOL[fmt]
+
+
+def _pair_tau_run(cuda, X, t1, t2, fmt):
+    """out[r, i, j] = sum_ef tau_ijef X[r.., e, f] through MixedResidual.pair_tau."""
+    from types import SimpleNamespace
+    from pycc_gb300.mixed import MixedResidual
+    no, nv = t1.shape
+    V = torch.zeros(nv, nv, nv, nv, dtype=torch.float64, device=cuda)  # only its strides
+    w = SimpleNamespace(device1=cuda, stream=None, no=no, nv=nv, vvvv_fp8=True,
+                        switch_threshold=1e-5,
+                        H=SimpleNamespace(ERI=SimpleNamespace(blocks={"vvvv": V})))
+    eng = MixedResidual(w)
+    out = torch.ones(X.shape[:-2] + (no, no), dtype=torch.float64, device=cuda)
+    eng.pair_tau(X, "mbef", "ovvv", t1, t2, out, fmt)
+    torch.cuda.synchronize()
+    eng.tc.check_status()
+    return out
+
+
+@pytest.mark.parametrize("no,nv,nb", [(4, 24, 3), (5, 37, 2), (1, 9, 4), (6, 1, 5)])
+def test_pair_form_intermediate_exact_integers(cuda, no, nv, nb):
+    """Zmbij-shaped tau_ijef X_mbef (X without any symmetry) in the pair form, added into an
+    output of ones: exact on integer data in BF16, including no = 1 (no antisymmetric
+    pairs) and nv = 1 (no e < f pairs)."""
+    g = torch.Generator(device=cuda).manual_seed(no * nv + nb)
+    X = torch.randint(-2, 3, (no, nb, nv, nv), generator=g, device=cuda).double()
+    t2 = torch.randint(-2, 3, (no, no, nv, nv), generator=g, device=cuda).double()
+    t1 = torch.randint(-1, 2, (no, nv), generator=g, device=cuda).double()
+    t2 = (t2 + t2.permute(1, 0, 3, 2)).contiguous()
+    tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
+    ref = 1.0 + torch.einsum("ijef,mbef->mbij", tau, X)
+    assert torch.equal(_pair_tau_run(cuda, X, t1, t2, FMT_BF16), ref)
+
+
+@pytest.mark.parametrize("fmt", [FMT_BF16, FMT_BF16X3F, FMT_BF16X3S])
+def test_pair_form_intermediate_random(cuda, fmt):
+    g = torch.Generator(device=cuda).manual_seed(9)
+    no, nv = 6, 45
+    X = torch.randn(no, 7, nv, nv, generator=g, device=cuda, dtype=torch.float64)
+    t2 = 0.1 * torch.randn(no, no, nv, nv, generator=g, device=cuda, dtype=torch.float64)
+    t1 = 0.1 * torch.randn(no, nv, generator=g, device=cuda, dtype=torch.float64)
+    t2 = (t2 + t2.permute(1, 0, 3, 2)).contiguous()
+    tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
+    ref = torch.einsum("ijef,mbef->mbij", tau, X)
+    got = _pair_tau_run(cuda, X, t1, t2, fmt) - 1.0
+    assert frob(got, ref) < TOL[fmt]
