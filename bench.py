@@ -515,7 +515,7 @@ def main():
     ap.add_argument("--nv", type=int, default=300)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--fp64-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-terms", action="store_true")
     ap.add_argument("--force-mode", default=None, choices=[None, "bf16x3f", "bf16x3s", "bf16x3"],
@@ -813,6 +813,7 @@ def main():
                 "host_phases_ms": dict(zip(("h2d", "iterate", "diis", "d2h", "sync"),
                                            np.mean(e2e_host[-args.e2e_steps:], axis=0).round(2)
                                            .tolist())) if args.e2e_steps > 0 else None,
+                "step_ms": [round(sum(ph), 2) for ph in e2e_phases[-args.e2e_steps:]],
                 "ms_per_step": e2e_ms} if args.e2e_steps > 0 else None,
         "gpu_launches": launches, "clocks": clocks, "setup_s": setup_s,
         "gemm_ms_per_iter": gemm_ms,

@@ -230,8 +230,8 @@ int pcg_ladder_pm_assemble(const double* Gp, const double* Gm, long long no, lon
                            double* h, void* stream);
 
 /* pcg_pair_pm_assemble: the same pair form for the tau_ijef X_r,ef terms of the
- *   intermediates (Zmbij: tau_ijef <mb|ef>, pycc/ccwfn.py:707; Wmnij: tau_ijef <mn|ef>,
- *   pycc/ccwfn.py:596; 'ijef,mbef->mbij' / 'ijef,mnef->mnij' of ContractionBackend.__call__).
+ *   intermediates (Zmbij: tau_ijef <mb|ef>, pycc/ccwfn.py:715; Wmnij: tau_ijef <mn|ef>,
+ *   pycc/ccwfn.py:603; 'ijef,mbef->mbij' / 'ijef,mnef->mnij' of ContractionBackend.__call__).
  *   Gp: [no(no+1)/2][nrow] = 1/2 sum_{e<=f} T+_ij,ef (X_r,ef + X_r,fe) over the i <= j pairs
  *   (row-major, with 1/2 on e = f), Gm: [no(no-1)/2][nrow] = 1/2 sum_{e<f} T-_ij,ef
  *   (X_r,ef - X_r,fe) over the i < j pairs, so Gp + Gm = sum_ef tau_ijef X_r,ef and

@@ -23,7 +23,7 @@ import torch
 from . import _lib
 from .contract import contract_f64
 from .tc import (FMT_BF16, FMT_BF16X3, FMT_BF16X3F, FMT_BF16X3S, FMT_BF16X6, FMT_FP8, Operand,
-                 TCEngine, pack, static_pack_format)
+                 TCEngine, static_pack_format)
 
 
 class MixedResidual:
@@ -57,10 +57,9 @@ class MixedResidual:
         self.bad = 0
         self.history = []
         self.profile = None       # list of (subscripts, fmt, start, end) events when set
-        self._pairs = None        # output map of the i <= j pair terms
         self._pm = None           # offset tables of the ladder's pair form
         self._kpm = {}            # K pair tables of the pair-form intermediates, per block
-        self._hole_tab = None     # the pair columns of Wmnij for the hole ladder
+        self._hpm = None          # offset tables of the hole ladder's pair form
         self._r_seed = None
         self._blocks = None       # the integral blocks the caches were built from
 
@@ -165,18 +164,6 @@ class MixedResidual:
         return Operand.of(labels, self.w.H.L.blocks[pat], key=("L", pat))
 
     # -- the <ab|ef> ladder over i <= j pairs (pycc/ccwfn.py:931) ---------------------------
-    def _pair_tables(self):
-        """Output map of the i <= j pair terms: the pair columns' offsets in the half
-        residual and their weights (1/2 on i = j, which the symmetrisation doubles)."""
-        if self._pairs is None:
-            no, nv = self.w.no, self.w.nv
-            ii, jj = np.triu_indices(no)
-            cmap = (ii * no * nv * nv + jj * nv * nv).astype(np.int64)
-            csc = np.where(ii == jj, 0.5, 1.0)
-            dev = self.w.device1
-            self._pairs = (torch.from_numpy(cmap).to(dev), torch.from_numpy(csc).to(dev))
-        return self._pairs
-
     def _pm_tables(self, t1, t2, V):
         """Offset tables of the symmetric / antisymmetric pair form of the ladder
         (``ladder_pm``): rows of V+- over the a <= b / a < b pairs, K over the e <= f /
@@ -214,7 +201,45 @@ class MixedResidual:
         self._pm = (key, tabs)
         return tabs
 
-    def ladder_pm(self, t1, t2, r, fmt):
+    def _hole_pm_tables(self, t1, t2, W):
+        """Offset tables of the hole ladder's pair form (``ladder_pm`` with Wmnij): rows of
+        tau+- over the a <= b / a < b pairs and K over the m <= n / m < n pairs (sources
+        tau_mnab = t2_mnab + t_ma t_nb and tau_mnba), rows of W+- over the i <= j / i < j pairs
+        and K over the same (m, n) pairs (sources W_mnij and W_mnji, with 1/2 on m = n for
+        W+).  Offsets follow the tensors' own strides (t2 and W: [m, n, ., .]; t1: [m, a])."""
+        key = (tuple(W.stride()), tuple(t2.stride()), tuple(t1.stride()))
+        if self._hpm is not None and self._hpm[0] == key:
+            return self._hpm[1]
+        no, nv = self.w.no, self.w.nv
+        dev = self.w.device1
+        sw, s2, s1 = W.stride(), t2.stride(), t1.stride()
+        tabs = {}
+        for sign, k in (("+", 0), ("-", 1)):
+            a, b = np.triu_indices(nv, k)
+            m, n = np.triu_indices(no, k)
+            i, j = m, n                                          # the i <= j (i < j) pairs
+            ur = np.zeros((6, a.size), dtype=np.int64)           # tau rows: (a, b)
+            ur[0] = a * s2[2] + b * s2[3]                        # t2_mnab
+            ur[1] = b * s2[2] + a * s2[3]                        # t2_mnba
+            ur[2], ur[3] = a * s1[1], b * s1[1]                  # t_ma t_nb
+            ur[4], ur[5] = b * s1[1], a * s1[1]                  # t_mb t_na
+            uk = np.zeros((6, m.size), dtype=np.int64)           # tau K: (m, n)
+            uk[0] = uk[1] = m * s2[0] + n * s2[1]
+            uk[2], uk[3] = m * s1[0], n * s1[0]
+            uk[4], uk[5] = m * s1[0], n * s1[0]
+            wr = np.zeros((6, i.size), dtype=np.int64)           # W rows: (i, j)
+            wr[0] = i * sw[2] + j * sw[3]                        # W_mnij
+            wr[1] = j * sw[2] + i * sw[3]                        # W_mnji
+            wk = np.zeros((6, m.size), dtype=np.int64)
+            wk[0] = wk[1] = m * sw[0] + n * sw[1]
+            kw = np.where(m == n, 0.5, 1.0).astype(np.float32) if sign == "+" else None
+            t = lambda x: torch.from_numpy(x).to(dev) if x is not None else None
+            tabs[sign] = {"urow": t(ur), "uk": t(uk), "wrow": t(wr), "wk": t(wk), "kw": t(kw),
+                          "rows": a.size, "cols": i.size, "k": m.size}
+        self._hpm = (key, tabs)
+        return tabs
+
+    def ladder_pm(self, t1, t2, r, fmt, Wmnij=None, hole_fmt=None):
         """r_ijab += 1/2 tau_ijef <ab|ef> (pycc/ccwfn.py:931) in symmetric / antisymmetric
         pair form: two GEMMs, G+- = T+- . V+-, over the e <= f (e < f) pairs of K, the
         a <= b (a < b) pairs of rows and the i <= j (i < j) pairs of columns, then
@@ -223,7 +248,14 @@ class MixedResidual:
         and S / 2 for i = j, as the i <= j pair form of the ladder does.
         T+-_ij,ef = tau_ijef +- tau_ijfe (packed from t2 and t1 in one pass), V+-_ab,ef =
         <ab|ef> +- <ab|fe> (packed once per format and cached).  Half of the i <= j pair
-        form's tensor-core work, and half of its packed integral bytes."""
+        form's tensor-core work, and half of its packed integral bytes.
+
+        With ``Wmnij`` the hole ladder r_ijab += 1/2 tau_mnab W_mnij (pycc/ccwfn.py:930) joins
+        the same G+-: tau_nmab = tau_mnba and W_nmij = W_mnji, so over the m <= n (m < n)
+        pairs sum_mn tau_mnab W_mnij = 1/2 (H+ + H-) with H+- = sum (tau_mnab +- tau_mnba)
+        (W_mnij +- W_mnji) (1/2 on m = n for +), which has the symmetry of G+- under
+        i<->j and a<->b.  Two small GEMMs (K = the occupied pairs, in ``hole_fmt``)
+        accumulate into G+- before the one assembly."""
         if not r.is_contiguous():
             raise ValueError("ladder_pm: the half residual must be contiguous")
         no, nv = self.w.no, self.w.nv
@@ -248,6 +280,20 @@ class MixedResidual:
             self.tc.run_gemm('ijef,abef->ijab' + sign, fmt, pa, pb, out, ['p'], ['q'], 'qp',
                              0.5, 0.0)
             G[sign] = out
+            if Wmnij is not None:
+                hb = self._hole_pm_tables(t1, t2, Wmnij)[sign]
+                if hb["k"] == 0:
+                    continue
+                hf = fmt if hole_fmt is None else hole_fmt
+                uop = Operand('mnab', (t2, 'mnab'), a=1.0, Y=(t2, 'mnba'), b=c, P=(t1, 'ma'),
+                              Q=(t1, 'nb'), c=1.0, R=(t1, 'mb'), S=(t1, 'na'), d=c)
+                pu = self.tc._pack(uop, ['a', 'b'], ['m', 'n'], hf, 'A', row_tab=hb["urow"],
+                                   k_tab=hb["uk"])
+                wop = Operand('mnij', (Wmnij, 'mnij'), a=1.0, Y=(Wmnij, 'mnji'), b=c)
+                pw = self.tc._pack(wop, ['i', 'j'], ['m', 'n'], hf, 'B', row_tab=hb["wrow"],
+                                   k_tab=hb["wk"], k_w=hb["kw"])
+                self.tc.run_gemm('mnab,mnij->ijab' + sign, hf, pu, pw, out, ['p'], ['q'], 'qp',
+                                 0.5, 1.0)
         _lib.call("pcg_ladder_pm_assemble", G["+"].data_ptr(),
                   G["-"].data_ptr() if G["-"] is not None else None, no, nv, r.data_ptr(),
                   _lib.stream_handle(self.w.stream))
@@ -283,8 +329,8 @@ class MixedResidual:
         ``pcg_pair_pm_assemble`` adds out_rij += G+ + G-, out_rji += G+ - G- (i < j) and
         out_rii += G+.  T+- are the ladder's own packed operands (packed once per residual
         call); X's pair combinations are packed once per format.  Half the tensor-core work
-        of the plain contraction (Zmbij: tau_ijef <mb|ef>, pycc/ccwfn.py:707; Wmnij:
-        tau_ijef <mn|ef>, pycc/ccwfn.py:596)."""
+        of the plain contraction (Zmbij: tau_ijef <mb|ef>, pycc/ccwfn.py:715; Wmnij:
+        tau_ijef <mn|ef>, pycc/ccwfn.py:603)."""
         if not out.is_contiguous():
             raise ValueError("pair_tau: the output must be contiguous")
         no = self.w.no
@@ -318,36 +364,11 @@ class MixedResidual:
                   G["-"].data_ptr() if G["-"] is not None else None, no, nrow, out.data_ptr(),
                   _lib.stream_handle(self.w.stream))
 
-    def hole_ladder_pairs(self, t1, t2, Wmnij, r):
-        """r_ijab += 1/2 tau_mnab W_mnij (pycc/ccwfn.py:930) through the i <= j pairs only.
-
-        W_nmji = W_mnij and tau_nmba = tau_mnab, so the term is symmetric under
-        (i<->j, a<->b), as the particle ladder is: the i <= j output map and 1/2 diagonal
-        weights of ``_pair_tables`` apply, with a row table selecting the pair columns of
-        W_mnij (offsets from W_mnij's own strides, so any layout of it is read correctly).
-        """
-        if not r.is_contiguous():
-            raise ValueError("hole_ladder_pairs: the half residual must be contiguous")
-        no = self.w.no
-        sw = tuple(Wmnij.stride())
-        if self._hole_tab is None or self._hole_tab[0] != sw:
-            ii, jj = np.triu_indices(no)
-            tab = np.zeros((6, ii.size), dtype=np.int64)
-            tab[0] = ii * sw[2] + jj * sw[3]             # Wmnij[m, n, i, j]
-            self._hole_tab = (sw, torch.from_numpy(tab).to(self.w.device1))
-        cmap, csc = self._pair_tables()
-        fmt = self.fmt()
-        tau = Operand('mnab', (t2, 'mnab'), P=(t1, 'ma'), Q=(t1, 'nb'), c=1.0)
-        pa = self.tc._pack(tau, ['a', 'b'], ['m', 'n'], fmt, 'A')
-        pb = pack(Operand.of('mnij', Wmnij), ['i', 'j'], ['m', 'n'], fmt, self.w.stream,
-                  row_tab=self._hole_tab[1])
-        self.tc.run_gemm('mnab,mnij->ijab', fmt, pa, pb, r, ['a', 'b'], [], 'ijab', 1.0, 1.0,
-                         col_map=cmap, col_scale=csc)
-
     def timed(self, name, fn, *args):
         """Run one term; with ``self.profile`` set, CUDA events on the launching stream
         around it (pack + GEMM + assembly) join the per-term table, and an NVTX range named
-        ``name`` ("ladder", "hole_ladder") selects its launches for profilers."""
+        ``name`` ("ladder": both ladders' GEMMs and their assembly) selects its launches for
+        profilers."""
         torch.cuda.nvtx.range_push(name)
         if self.profile is None:
             fn(*args)
@@ -454,8 +475,7 @@ class MixedResidual:
         contract_f64('je,me->mj', t1, Fme, out=Fmj, alpha=0.5, beta=1.0)
         self.tcc('imab,mj->ijab', Operand.of('imab', t2), Operand.of('mj', Fmj), r, alpha=-1.0)
         # ladders
-        self.timed("hole_ladder", self.hole_ladder_pairs, t1, t2, Wmnij, r)
-        self.timed("ladder", self.ladder_pm, t1, t2, r, self.ladder_fmt())
+        self.timed("ladder", self.ladder_pm, t1, t2, r, self.ladder_fmt(), Wmnij, self.fmt())
         # - t_ma (Z_mbij + <mb|ij>) - t_ie t_ma <mb|ej> - t_ie t_mb <ma|je>, the last written
         # as its (i<->j, a<->b) image - t_je t_ma <mb|ie>, which the symmetrisation
         # r2 = h + h' sums to the same residual; the o^3 v tensors are summed in Zmbij
