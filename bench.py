@@ -515,7 +515,7 @@ def main():
     ap.add_argument("--nv", type=int, default=300)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--fp64-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-terms", action="store_true")
     ap.add_argument("--force-mode", default=None, choices=[None, "bf16x3f", "bf16x3s", "bf16x3"],

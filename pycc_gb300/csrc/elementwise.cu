@@ -368,33 +368,39 @@ __device__ __forceinline__ void df_term(double x, float ch, float cl, float& S, 
 }
 
 // Two elements per step through 16-byte loads (the inputs and the output are 16-byte
-// aligned, checked by the host); the last element of an odd n is done by one thread.
+// aligned, checked by the host).  All k loads of a step are issued before its arithmetic
+// (KMAX bounds k at compile time, so the loaded values stay in registers); the
+// coefficients' FP32 pieces live in shared memory.  The last element of an odd n is done
+// by one thread.
+template <int KMAX>
 __global__ void lincomb_df_kernel(VecList xs, int k, long long n, double* __restrict__ out) {
-  float ch[kMaxVec], cl[kMaxVec];
-#pragma unroll
-  for (int j = 0; j < kMaxVec; ++j) {
-    ch[j] = (float)xs.c[j];
-    cl[j] = (float)(xs.c[j] - (double)ch[j]);
+  __shared__ float sch[kMaxVec], scl[kMaxVec];
+  if (threadIdx.x < kMaxVec) {
+    const float h = (float)xs.c[threadIdx.x];
+    sch[threadIdx.x] = h;
+    scl[threadIdx.x] = (float)(xs.c[threadIdx.x] - (double)h);
   }
+  __syncthreads();
   const long long n2 = n >> 1;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n2;
        q += (long long)gridDim.x * blockDim.x) {
+    double2 x[KMAX];
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j)
+      if (j < k) x[j] = reinterpret_cast<const double2*>(xs.p[j])[q];
     float S0 = 0.f, E0 = 0.f, S1 = 0.f, E1 = 0.f;
 #pragma unroll
-    for (int j = 0; j < kMaxVec; ++j)
+    for (int j = 0; j < KMAX; ++j)
       if (j < k) {
-        const double2 x = reinterpret_cast<const double2*>(xs.p[j])[q];
-        df_term(x.x, ch[j], cl[j], S0, E0);
-        df_term(x.y, ch[j], cl[j], S1, E1);
+        df_term(x[j].x, sch[j], scl[j], S0, E0);
+        df_term(x[j].y, sch[j], scl[j], S1, E1);
       }
     reinterpret_cast<double2*>(out)[q] =
         make_double2(f32_to_f64(S0) + f32_to_f64(E0), f32_to_f64(S1) + f32_to_f64(E1));
   }
   if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
     float S = 0.f, E = 0.f;
-#pragma unroll
-    for (int j = 0; j < kMaxVec; ++j)
-      if (j < k) df_term(xs.p[j][n - 1], ch[j], cl[j], S, E);
+    for (int j = 0; j < k; ++j) df_term(xs.p[j][n - 1], sch[j], scl[j], S, E);
     out[n - 1] = f32_to_f64(S) + f32_to_f64(E);
   }
 }
@@ -597,8 +603,14 @@ extern "C" int pcg_lincomb_f64_df(const double* const* xs, const double* c, int 
     set_error("pcg_lincomb_f64_df: vectors must be 16-byte aligned");
     return -1;
   }
-  lincomb_df_kernel<<<ew_blocks(std::max(n / 2, 1LL)), EW_THREADS, 0, (cudaStream_t)stream>>>(
-      v, k, n, out);
+  const int nb = ew_blocks(std::max(n / 2, 1LL));
+  cudaStream_t st = (cudaStream_t)stream;
+  if (k <= 4)
+    lincomb_df_kernel<4><<<nb, EW_THREADS, 0, st>>>(v, k, n, out);
+  else if (k <= 8)
+    lincomb_df_kernel<8><<<nb, EW_THREADS, 0, st>>>(v, k, n, out);
+  else
+    lincomb_df_kernel<kMaxVec><<<nb, EW_THREADS, 0, st>>>(v, k, n, out);
   PCG_CHECK_LAUNCH("pcg_lincomb_f64_df");
   return 0;
 }

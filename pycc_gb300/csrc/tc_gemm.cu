@@ -56,6 +56,7 @@ struct Args {
   long long mt, nt;  // output tiles along M and N
   int gm;            // M tiles per raster group (see decode_tile)
   int bs;            // columns per N tile: BN or less, a multiple of 16 (see pcg_tc_gemm)
+  int stage_bytes;   // bytes TMA delivers per ring stage: the A tile and bs rows of B
   int splits;        // K splits across CTAs (FP64 atomics in the epilogue when > 1)
   int kb_per_split;  // K blocks of one split
   int nkb_total;     // K blocks of the whole K range
@@ -296,7 +297,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1)
                 stop = true;
                 break;
               }
-              mbar_expect_tx(&full[s], L::STAGE);
+              mbar_expect_tx(&full[s], (uint32_t)p.stage_bytes);
 #pragma unroll
               for (int q = 0; q < NP; ++q) {
                 const CUtensorMap* ta = &maps.a[NP == 1 ? p.pt.a[pass] : q];
@@ -1179,9 +1180,13 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   long long tiles = mt * nt;
   int splits = 1;
   const int sms = num_sms();
+  // K splits for a launch with fewer tiles than SMs: as many as keep every (tile, split)
+  // on its own SM in one wave -- a split count that overfills the wave by even one tile
+  // makes one CTA run two and doubles the launch (3 tiles x 51 splits on 152 SMs) -- and
+  // each split at least 4 K blocks long
   if (tiles < sms && nkb >= 8) {
-    splits = (int)std::min<long long>((sms + tiles - 1) / tiles, nkb / 4);
-    splits = std::max(1, std::min(splits, 64));
+    splits = (int)std::min<long long>(sms / tiles, nkb / 4);
+    splits = std::max(1, splits);
   }
   int kps = (nkb + splits - 1) / splits;
   splits = (nkb + kps - 1) / kps;
@@ -1197,6 +1202,9 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
     const long long units = (N + 15) / 16;
     a.bs = (int)(16 * ((units + nt - 1) / nt));
   }
+  // B's tensor map box is bs rows high (a narrower tile loads no rows it does not multiply);
+  // the stage's B slot keeps BN rows
+  a.stage_bytes = (fmt == kBF16x3F || fmt == kBF16x3S ? 2 : 1) * (BM + a.bs) * KBYTES;
   // raster group: a wave of W CTAs touches gm A row blocks (BM rows) and W / gm B row
   // blocks (BN rows); gm = sqrt(W BN / BM) minimises their sum.  A narrow N (nt <= W / gm)
   // keeps the N-fastest order (gm = 1): the CTAs sharing an A row block are then adjacent
@@ -1233,7 +1241,7 @@ extern "C" int pcg_tc_gemm(int fmt, const void* A_hi, const void* A_mid, const v
   const void* pb[3] = {B_hi, fmt == kBF16x6 ? B_mid : B_lo, B_lo};
   for (int q = 0; q < 3; ++q) {
     if (!make_map(&maps.a[q], pa[q] ? pa[q] : A_hi, M, lda * eb, Kp * eb, eb, BM)) return -1;
-    if (!make_map(&maps.b[q], pb[q] ? pb[q] : B_hi, N, ldb * eb, Kp * eb, eb, BN)) return -1;
+    if (!make_map(&maps.b[q], pb[q] ? pb[q] : B_hi, N, ldb * eb, Kp * eb, eb, a.bs)) return -1;
   }
   if (split_acc) {
     switch (BN) {
