@@ -2,9 +2,9 @@
 points (``tests/abi_model.py``) with the tensor-core pack and GEMM in exact FP64.
 
 Every contraction the engine plans -- operand combinations folded into packs (tau, 2 t2 -
-t2~, W + W~), K orders, the i <= j pair rows of the <ab|ef> ladder with their output map and
-1/2 diagonal weights, the o^3 v tensors summed into Zmbij, the symmetrisation images -- is
-checked exactly: with no format rounding, each precision stage's residual must equal the
+t2~, W + W~), K orders, the symmetric / antisymmetric pair forms of the two ladders and of
+Zmbij's and Wmnij's tau terms with their offset tables, K weights and assemblies, the o^3 v
+tensors summed into Zmbij, the symmetrisation images -- is checked exactly: with no format rounding, each precision stage's residual must equal the
 reference's FP64 residual (o5v19.npz) to rounding.  The formats' own accuracy is the subject
 of the ``-m gpu`` tests.
 """
