@@ -131,3 +131,30 @@ def test_degenerate_sizes(model, no, nv, precision):
             r1, r2 = w.residuals(w.H.F, torch.from_numpy(t1), torch.from_numpy(t2))
             assert rel(r1, want1) < 1e-12 and rel(r2, want2) < 1e-12, stage
     assert torch.equal(w.H.F, F0)
+
+
+@pytest.mark.parametrize("no,nv,nb", [(4, 6, 3), (1, 5, 2), (3, 1, 4)])
+def test_pair_form_intermediate_through_the_model(model, no, nv, nb):
+    """MixedResidual.pair_tau (Zmbij / Wmnij's tau_ijef X_r,ef in symmetric / antisymmetric
+    pair form, with its tables, K weights and pcg_pair_pm_assemble) equals the plain
+    contraction in the exact FP64 model, including no = 1 (no i < j pairs) and nv = 1 (no
+    e < f pairs)."""
+    from types import SimpleNamespace
+    from pycc_gb300.mixed import MixedResidual
+    from pycc_gb300.tc import FMT_BF16X3F
+    rng = np.random.default_rng(no * 100 + nv * 10 + nb)
+    X = torch.from_numpy(rng.standard_normal((no, nb, nv, nv)))
+    t1 = torch.from_numpy(0.1 * rng.standard_normal((no, nv)))
+    t2 = 0.1 * rng.standard_normal((no, no, nv, nv))
+    t2 = torch.from_numpy(t2 + t2.transpose(1, 0, 3, 2)).contiguous()
+    V = torch.zeros(nv, nv, nv, nv, dtype=torch.float64)
+    w = SimpleNamespace(device1="cpu", stream=None, no=no, nv=nv, vvvv_fp8=True,
+                        switch_threshold=1e-5,
+                        H=SimpleNamespace(ERI=SimpleNamespace(blocks={"vvvv": V})))
+    eng = MixedResidual(w)
+    out = torch.ones((no, nb, no, no), dtype=torch.float64)
+    eng.pair_tau(X, "mbef", "ovvv", t1, t2, out, FMT_BF16X3F)
+    tau = t2 + t1[:, None, :, None] * t1[None, :, None, :]
+    ref = 1.0 + torch.einsum("ijef,mbef->mbij", tau, X)
+    assert torch.allclose(out, ref, rtol=0, atol=1e-13)
+    assert "pcg_pair_pm_assemble" in model.calls
