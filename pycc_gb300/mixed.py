@@ -454,8 +454,10 @@ class MixedResidual:
         t2s = Operand('imae', (t2, 'imae'), a=2.0, Y=(t2, 'imea'), b=-1.0)
         self.tcc('imae,me->ia', t2s, Operand.of('me', Fme), r)
         self.tcc('nf,nafi->ia', Operand.of('nf', t1), self.ll('ovvo', 'nafi'), r)
-        t2s = Operand('mief', (t2, 'mief'), a=2.0, Y=(t2, 'mife'), b=-1.0)
-        self.tcc('mief,maef->ia', t2s, self.eri('ovvv', 'maef'), r)
+        # (2 t2_mief - t2_mife) <ma|ef> summed over e, f is t2_mief (2 <ma|ef> - <ma|fe>)
+        # = t2_mief L_maef (pycc/ccwfn.py:759): the resident L block takes the combination,
+        # and t2 is gathered once instead of twice (once transposed)
+        self.tcc('mief,maef->ia', Operand.of('mief', t2), self.ll('ovvv', 'maef'), r)
         self.tcc('mnae,nmei->ia', Operand.of('mnae', t2), self.ll('oovo', 'nmei'), r, alpha=-1.0)
         return r
 
