@@ -64,6 +64,16 @@ def _f64(what, *ts):
             raise TypeError("%s: float64 tensors expected, got %s" % (what, t.dtype))
 
 
+def _reference_wfn(w):
+    """True for an object shaped like the reference's wave function: an integer ``no`` and an
+    ``H`` whose ``F`` and ``ERI`` are full MO arrays (numpy or torch)."""
+    H = getattr(w, 'H', None)
+    no = getattr(w, 'no', None)
+    F, ERI = getattr(H, 'F', None), getattr(H, 'ERI', None)
+    return (isinstance(no, (int, np.integer)) and hasattr(F, 'shape') and hasattr(ERI, 'shape')
+            and len(F.shape) == 2 and len(ERI.shape) == 4)
+
+
 class CCwfn:
     """RHF-CCSD wave function on one GPU (mirrors ``pycc/ccwfn.py:32-213``).
 
@@ -118,8 +128,16 @@ class CCwfn:
             raise PyCCError("Unknown keyword argument(s): %s" % ", ".join(sorted(kwargs)))
 
         H = scf_wfn if isinstance(scf_wfn, Hamiltonian) else getattr(scf_wfn, 'H', None)
+        if not isinstance(H, Hamiltonian) and _reference_wfn(scf_wfn):
+            # a reference-style wave function (pycc's own CCwfn, for one): its MO Hamiltonian
+            # (full F, ERI and L arrays, pycc/hamiltonian.py) and its active occupied count
+            dev = getattr(scf_wfn, 'device1', None)
+            dev = dev if isinstance(dev, torch.device) else torch.device('cuda:0')
+            H = Hamiltonian.from_arrays(H.F, H.ERI, int(scf_wfn.no), L=getattr(H, 'L', None),
+                                        device=dev)
         if not isinstance(H, Hamiltonian):
-            raise TypeError("CCwfn needs a pycc_gb300.Hamiltonian (or an object carrying one as .H)")
+            raise TypeError("CCwfn needs a pycc_gb300.Hamiltonian, an object carrying one as .H, "
+                            "or a reference-style wave function (.no and .H with F and ERI)")
         _lib.load()
         self.H = H
         self.no, self.nv, self.nmo = H.no, H.nv, H.nmo

@@ -98,3 +98,22 @@ def test_reference_constructor_options(model, ham_o5v19):
         pg.CCwfn(H, frozen_core=True)
     with pytest.raises(pg.PyCCError):
         pg.CCwfn(H, no_such_option=1)
+
+
+def test_reference_style_wavefunction(model, ham_o5v19, golden_o5v19):
+    """CCwfn accepts a wave function shaped like the reference's (an active occupied count
+    ``no`` and ``H`` with the full F, ERI and L arrays, as pycc's own CCwfn carries them): it
+    uploads the blocks itself, and the residual equals the reference's."""
+    from types import SimpleNamespace
+    _, F, ERI, L = ham_o5v19
+    g = golden_o5v19
+    ref_like = SimpleNamespace(no=5, eref=-1.5, device1=torch.device("cpu"),
+                               H=SimpleNamespace(F=F, ERI=ERI, L=L))
+    w = pg.CCwfn(ref_like, precision="DP")
+    assert w.no == 5 and w.nv == 19 and w.eref == -1.5
+    r1, r2 = w.residuals(w.H.F, torch.from_numpy(g["probe_t1"].copy()),
+                         torch.from_numpy(g["probe_t2"].copy()))
+    assert np.abs(r1.numpy() - g["r1"]).max() / np.abs(g["r1"]).max() < 1e-12
+    assert np.abs(r2.numpy() - g["r2"]).max() / np.abs(g["r2"]).max() < 1e-12
+    with pytest.raises(TypeError):
+        pg.CCwfn(SimpleNamespace(no=5, H=SimpleNamespace(F=F)), precision="DP")
