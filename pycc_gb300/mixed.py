@@ -13,7 +13,10 @@ FP64 (the GEMM epilogue accumulates into FP64).  Matrix-vector shaped and O(o^2 
 run on the FP64 kernels.  Two algebraically exact refactorings are shared with the FP64 path:
 the t1 t1 <mb|ej> / <ma|je> terms of r2 are evaluated in two O(o^3 v^2) steps instead of one
 O(o^3 v^3) step, and the Fme dressings of Fae / Fmi are folded into the dressed
-one-body matrices before they multiply t2.
+one-body matrices before they multiply t2.  Exact rearrangements of this path alone: the
+particle and hole ladders and the tau terms of Wmnij and Zmbij in symmetric /
+antisymmetric pair form (``ladder_pm``, ``pair_tau``), the ring terms regrouped, and r_T1's
+(2 t2 - t2~) <ma|ef> as t2 L_maef.
 """
 from __future__ import annotations
 
@@ -32,9 +35,10 @@ class MixedResidual:
     A stage hands over to the next when the update norm drops below its threshold or
     stops decreasing (the stage's rounding floor): ``fp8_threshold`` (1e-3) for the FP8
     stage, ``switch_threshold`` (1e-5) for BF16.  The fused split-BF16x3 stage (all three
-    products from one shared-memory stage) runs until its floor; the last stage issues the
-    products as separate passes, whose FP32 chains carry less truncation bias, and
-    fixes the converged energy.
+    products from one shared-memory stage, one FP32 accumulator) runs until its floor; the
+    last stage keeps the two small products in an accumulator of their own over the tile's
+    whole K, whose FP32 chain then carries less truncation bias, and fixes the converged
+    energy.
     """
 
     STALL_RATIO = 0.8     # rms above this fraction of the stage's best counts as no progress
