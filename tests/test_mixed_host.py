@@ -158,3 +158,24 @@ def test_pair_form_intermediate_through_the_model(model, no, nv, nb):
     ref = 1.0 + torch.einsum("ijef,mbef->mbij", tau, X)
     assert torch.allclose(out, ref, rtol=0, atol=1e-13)
     assert "pcg_pair_pm_assemble" in model.calls
+
+
+@pytest.mark.parametrize("no,nv", [(1, 4), (2, 1), (1, 1)])
+def test_degenerate_pair_counts_vs_oracle(model, no, nv):
+    """The pair forms with empty antisymmetric parts (no = 1: no i < j or m < n pairs;
+    nv = 1: no a < b or e < f pairs) in the full mixed residual, every stage, against the
+    oracle."""
+    fac = pg.SyntheticFactors(no, nv, 3)
+    F, ERI, L = fac.hamiltonian()
+    w = pg.CCwfn(pg.Hamiltonian.from_arrays(F, ERI, no, L=L, device="cpu"), precision="MIXED")
+    rng = np.random.default_rng(no + 10 * nv)
+    t1 = 0.05 * rng.standard_normal((no, nv))
+    t2 = 0.05 * rng.standard_normal((no, no, nv, nv))
+    t2 = t2 + t2.transpose(1, 0, 3, 2)
+    o, v = slice(0, no), slice(no, no + nv)
+    want1, want2 = oc.residuals(o, v, F, ERI, L, t1, t2)
+    eng = w.mixed_engine()
+    for stage in range(len(eng.stages)):
+        eng.stage = stage
+        r1, r2 = w.residuals(w.H.F, torch.from_numpy(t1), torch.from_numpy(t2))
+        assert rel(r1, want1) < 1e-13 and rel(r2, want2) < 1e-13, eng.stages[stage]
