@@ -93,6 +93,33 @@ def test_static_and_dynamic_caches(recorder):
     assert any(s is t1 for s in entry[1])
 
 
+def test_dynamic_cache_keys_the_gather_not_the_labels(recorder):
+    """Spellings of one gather (the same tensor, extents and strides per row and K index,
+    under other label names or with the K order following the source's strides) share a pack
+    within a residual; a different combination coefficient or transposed rows do not."""
+    o, v = 3, 5
+    eng = TCEngine("cpu")
+    eng.dyn_cache = {}
+    x = t(o, o, v, v)
+    V = Operand.of("mbef", t(o, v, v, v), key=("ERI", "ovvv"))
+    n0 = len(recorder["pack"])
+    eng.contract("ijef,mbef->mbij", Operand.of("ijef", x), V, t(o, v, o, o), fmt=FMT_BF16X3)
+    eng.contract("klef,mbef->mbkl", Operand.of("klef", x), V, t(o, v, o, o), fmt=FMT_BF16X3)
+    dyn = [c for c in recorder["pack"][n0:] if c[4] is None]
+    assert len(dyn) == 1
+    # x read as x[i, j, f, e]: K runs (f, e) by the source's strides, the same bytes
+    eng.contract("ijef,mbef->mbij", Operand("ijef", (x, "ijfe")), V, t(o, v, o, o),
+                 fmt=FMT_BF16X3)
+    dyn = [c for c in recorder["pack"][n0:] if c[4] is None]
+    assert len(dyn) == 1
+    eng.contract("ijef,mbef->mbij", Operand("ijef", (x, "ijef"), a=2.0), V, t(o, v, o, o),
+                 fmt=FMT_BF16X3)
+    eng.contract("ijef,mbef->mbij", Operand("ijef", (x, "jief")), V, t(o, v, o, o),
+                 fmt=FMT_BF16X3)
+    dyn = [c for c in recorder["pack"][n0:] if c[4] is None]
+    assert len(dyn) == 3
+
+
 def test_static_pack_formats():
     assert static_pack_format(FMT_BF16) == FMT_BF16X3
     assert static_pack_format(FMT_BF16X3F) == FMT_BF16X3
